@@ -1,0 +1,484 @@
+#!/usr/bin/env python
+"""Benchmark of the batched FP32 transform path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload cfg2|cfg1|cfg3|cfg4]
+
+Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
+round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
+x ~ N(0,1) float32, loss = sum(w*|X|^2) with w ~ U[0,1].  One step runs,
+for each N: X = R2C(x), y = C2R(X), G = 2*w*X (the loss gradient, one torch
+elementwise kernel) and dx = R2C-adjoint(G).  `value` counts the
+algorithmic bytes of the transforms only (one read of each transform's
+input + one write of its output) per second of the whole step.
+
+Timing: inputs resident in HBM, rotating buffer sets whose total exceeds
+2x the L2 size, W warm-up steps, K timed steps between barriers and device
+synchronisation, CUDA events on the launch stream, max over ranks.
+`roofline` times every launch of the dominant kernel (R2C, N=3000) with
+CUDA events on its stream; `e2e` repeats the step through the C ABI with
+host (pinned) buffers, so the host<->device copies are inside the timing;
+`cpu_baseline` times the FP32 port of the reference's CPU-side algorithm
+(oracle port) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ops-fft_gb300"))
+
+METRIC = "Batched C2C/R2C GB/s & % HBM roofline; split-TC vs FP32 Stockham at 1e-6 err"
+FALLBACK_HBM_GBS = 6800.0
+
+# DRAM traffic per launch of the dominant kernel measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum), summarised under profiles/.
+NCU_TRAFFIC = {}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", FALLBACK_HBM_GBS)), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during timing."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = []
+        with open(self.tmp.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.tmp.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- workloads
+class Cfg2:
+    """R2C -> C2R round trip with gradients, N in (3000, 1024), batch 4096."""
+
+    name = "r2c_c2r_roundtrip_grad"
+
+    def __init__(self, torch, A, dev, stream, nsets):
+        self.torch, self.A = torch, A
+        self.sizes = (3000, 1024)
+        self.batch = 4096
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        self.sets = []
+        self.plans = {}
+        for n in self.sizes:
+            pr = A.Plan.plan1d(n, A.R2C, self.batch)
+            pc = A.Plan.plan1d(n, A.C2R, self.batch)
+            pr.set_stream(stream)
+            pc.set_stream(stream)
+            self.plans[n] = (pr, pc)
+        for _ in range(nsets):
+            s = {}
+            for n in self.sizes:
+                nb = n // 2 + 1
+                x = torch.randn((self.batch, n), generator=g).to(dev)
+                w2 = (2 * torch.rand((self.batch, nb), generator=g)).to(dev)
+                s[n] = dict(x=x, w2=w2, X=torch.empty((self.batch, nb), dtype=torch.complex64, device=dev),
+                            y=torch.empty_like(x), G=torch.empty((self.batch, nb), dtype=torch.complex64, device=dev),
+                            gx=torch.empty_like(x))
+            self.sets.append(s)
+        self.bytes_per_transform = {n: self.batch * (n * 4 + (n // 2 + 1) * 8) for n in self.sizes}
+        self.alg_bytes_per_step = sum(3 * b for b in self.bytes_per_transform.values())
+        self.launches_per_step = 3 * len(self.sizes)
+        self.dominant = ("R2C N=3000 batch=4096 (fused even/odd post-process)", self.bytes_per_transform[3000])
+        self.set_bytes = sum(t.numel() * t.element_size() for t in self.sets[0][3000].values()) + sum(
+            t.numel() * t.element_size() for t in self.sets[0][1024].values())
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        for n in self.sizes:
+            b = s[n]
+            pr, pc = self.plans[n]
+            if dom_events is not None and n == 3000:
+                e0, e1 = dom_events
+                e0.record()
+                pr.exec_r2c(b["x"], b["X"])
+                e1.record()
+            else:
+                pr.exec_r2c(b["x"], b["X"])
+            pc.exec_c2r(b["X"], b["y"])
+            self.torch.mul(b["X"], b["w2"], out=b["G"])
+            pr.exec_r2c_adjoint(b["G"], b["gx"])
+
+    # host-buffer variant through the same C ABI (the reference's calling
+    # convention: host pointers in and out, return means done)
+    def make_host(self):
+        torch = self.torch
+        self.host = {}
+        for n in self.sizes:
+            s = self.sets[0][n]
+            self.host[n] = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s.items()}
+            for k, v in s.items():
+                self.host[n][k].copy_(v.cpu())
+            self.host[n]["G"].copy_(self.host[n]["X"] * 0 + 1)
+        h2d = sum(self.host[n][k].numel() * self.host[n][k].element_size()
+                  for n in self.sizes for k in ("x", "X", "G"))
+        d2h = sum(self.host[n][k].numel() * self.host[n][k].element_size()
+                  for n in self.sizes for k in ("X", "y", "gx"))
+        return h2d, d2h
+
+    def step_host(self):
+        for n in self.sizes:
+            h = self.host[n]
+            pr, pc = self.plans[n]
+            pr.exec_r2c(h["x"], h["X"])
+            pc.exec_c2r(h["X"], h["y"])
+            pr.exec_r2c_adjoint(h["G"], h["gx"])
+
+    # CPU baseline: FP32 port of the reference path on a sample of rows
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        done = 0
+        t0 = time.perf_counter()
+        for n in self.sizes:
+            x = rng.standard_normal((rows, n)).astype(np.float32)
+            X = O.port_r2c(x, nthreads)
+            O.port_c2r(X, n, nthreads)
+            Gh = X.copy()
+            Gh[:, 1:(n + 1) // 2] *= 0.5  # R2C adjoint = C2R of the halved interior bins
+            O.port_c2r(Gh, n, nthreads)
+            done += 3 * rows * (n * 4 + (n // 2 + 1) * 8)
+        return done, time.perf_counter() - t0
+
+    def config(self):
+        return {"workload": "1D R2C->C2R round trip with gradients (loss sum(w*|X|^2))", "n": list(self.sizes),
+                "batch": self.batch, "dtype": "float32 / complex64 interleaved",
+                "step": "per N: R2C, C2R, G=2wX (torch), R2C adjoint"}
+
+
+class C2CWorkload:
+    """Plain batched C2C (cfg1: 4096 x 256; cfg3: 65536 x 64 and 16384 x 64)."""
+
+    def __init__(self, torch, A, dev, stream, nsets, sizes, name, uniform):
+        self.torch, self.A = torch, A
+        self.sizes = sizes
+        self.name = name
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        self.plans = {}
+        self.sets = []
+        for n, b in sizes:
+            p = A.Plan.plan1d(n, A.C2C, b)
+            p.set_stream(stream)
+            self.plans[n] = p
+        for _ in range(nsets):
+            s = {}
+            for n, b in sizes:
+                if uniform:
+                    x = torch.complex(torch.rand((b, n), generator=g) * 2 - 1, torch.rand((b, n), generator=g) * 2 - 1)
+                else:
+                    x = torch.complex(torch.randn((b, n), generator=g), torch.randn((b, n), generator=g))
+                s[n] = dict(x=x.to(dev), y=torch.empty((b, n), dtype=torch.complex64, device=dev))
+            self.sets.append(s)
+        self.bytes_per_transform = {n: 16 * n * b for n, b in sizes}
+        self.alg_bytes_per_step = sum(self.bytes_per_transform.values())
+        self.launches_per_step = sum(len([1]) * self.plans[n].info().nsteps for n, _ in sizes)
+        n0 = sizes[0][0]
+        self.dominant = (f"C2C N={n0} batch={sizes[0][1]}", self.bytes_per_transform[n0])
+        self.dom_n = n0
+        self.set_bytes = sum(16 * n * b for n, b in sizes)
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        for n, _ in self.sizes:
+            if dom_events is not None and n == self.dom_n:
+                dom_events[0].record()
+                self.plans[n].exec_c2c(s[n]["x"], s[n]["y"], self.A.FORWARD)
+                dom_events[1].record()
+            else:
+                self.plans[n].exec_c2c(s[n]["x"], s[n]["y"], self.A.FORWARD)
+
+    def make_host(self):
+        torch = self.torch
+        self.host = {}
+        for n, _ in self.sizes:
+            s = self.sets[0][n]
+            self.host[n] = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s.items()}
+            self.host[n]["x"].copy_(s["x"].cpu())
+        b = sum(16 * n * bb for n, bb in self.sizes) // 2
+        return b, b
+
+    def step_host(self):
+        for n, _ in self.sizes:
+            self.plans[n].exec_c2c(self.host[n]["x"], self.host[n]["y"], self.A.FORWARD)
+
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        done = 0
+        t0 = time.perf_counter()
+        for n, b in self.sizes:
+            r = max(1, min(b, rows * 4096 // n))
+            x = (rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n))).astype(np.complex64)
+            O.port_c2c(x, -1, nthreads)
+            done += 16 * n * r
+        return done, time.perf_counter() - t0
+
+    def config(self):
+        return {"workload": self.name, "sizes": [list(s) for s in self.sizes], "dtype": "complex64 interleaved"}
+
+
+def make_workload(name, torch, A, dev, stream, nsets):
+    if name == "cfg2":
+        return Cfg2(torch, A, dev, stream, nsets)
+    if name == "cfg1":
+        return C2CWorkload(torch, A, dev, stream, nsets, [(4096, 256)], "1D C2C forward N=4096 batch=256", True)
+    if name == "cfg3":
+        return C2CWorkload(torch, A, dev, stream, nsets, [(65536, 64), (16384, 64)],
+                           "1D C2C forward N=65536,16384 batch=64 (FP32 Stockham form)", False)
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(wl, target_s=12.0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    cores = os.cpu_count() or 1
+    rows = 64
+    done, dt = wl.cpu_sample(O, rows, cores)  # warm-up and size probe
+    reps = max(1, int(target_s / max(dt, 1e-3)))
+    rows_total = rows
+    if dt < target_s / 20:
+        rows_total = min(rows * int(target_s / 4 / max(dt, 1e-3)), 4096)
+        reps = 2
+    done = 0
+    t = 0.0
+    for _ in range(reps):
+        d, dt = wl.cpu_sample(O, rows_total, cores)
+        done += d
+        t += dt
+    return {"value": round(done / t / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{rows_total} rows per transform length x {reps} repetitions of the FP32 port of the "
+                      f"reference's R2C/C2R/C2C algorithm (oracle/oracle_fft.c port_*), OpenMP over rows"}
+
+
+# ------------------------------------------------------------------- main
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg2")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    import aclfft as A
+
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    stream = torch.cuda.current_stream()
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    probe = make_workload(args.workload, torch, A, dev, stream, 1)
+    nsets = max(1, -(-2 * l2 // max(probe.set_bytes, 1)) + (1 if probe.set_bytes < 4 * l2 else 0))
+    del probe
+    torch.cuda.empty_cache()
+    wl = make_workload(args.workload, torch, A, dev, stream, nsets)
+
+    for i in range(args.warmup):
+        wl.step(i)
+    torch.cuda.synchronize()
+
+    nk = args.steps
+    dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0.record()
+    for i in range(nk):
+        wl.step(i, dom_ev[i])
+    t1.record()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1)
+    if dist:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    ms_per_step = ms / nk
+    value = wl.alg_bytes_per_step * world * nk / (ms / 1e3) / 1e9
+
+    dom_ms = statistics.mean(a.elapsed_time(b) for a, b in dom_ev)
+    peak, peak_kind = _peaks()
+    achieved = wl.dominant[1] / (dom_ms / 1e3) / 1e9
+    traffic = NCU_TRAFFIC.get((args.workload, "dominant"))
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "kernel": wl.dominant[0], "alg_bytes_per_launch": wl.dominant[1],
+                "avg_launch_us": round(dom_ms * 1e3, 2)}
+
+    e2e = None
+    if not args.no_e2e:
+        h2d, d2h = wl.make_host()
+        for _ in range(2):
+            wl.step_host()
+        torch.cuda.synchronize()
+        ke = max(3, min(nk, 10))
+        if dist:
+            dist.barrier()
+        ts = time.perf_counter()
+        for _ in range(ke):
+            wl.step_host()
+        torch.cuda.synchronize()
+        te = time.perf_counter() - ts
+        if dist:
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": round(wl.alg_bytes_per_step * world * ke / te / 1e9, 2), "unit": "GB/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "path": "aclfftExec* with pinned host buffers (library stages and synchronises)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(wl)
+
+    if rank == 0:
+        cfg = wl.config()
+        cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
+        cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": nk,
+                "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
+                "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": wl.launches_per_step * nk, "clocks": clk}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args, rank, world):
+    """The reference's own implementation of the path on the host cores.
+
+    The reference ships no CPU transform: its kernels are Ascend C and its
+    golden path is torch.fft.  The arm therefore runs the FP32 port of the
+    reference's arch35 algorithm (oracle/oracle_fft.c port_*) with all host
+    threads, on a bounded sample of the same workload per step.
+    """
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    class _Shim:
+        pass
+
+    torch = None
+    wlname = args.workload
+    if wlname == "cfg2":
+        wl = Cfg2.__new__(Cfg2)
+        wl.sizes = (3000, 1024)
+        wl.batch = 4096
+        cfg = Cfg2.config(wl)
+        sample = lambda rows, th: Cfg2.cpu_sample(wl, O, rows, th)
+    else:
+        wl = C2CWorkload.__new__(C2CWorkload)
+        wl.sizes = [(4096, 256)] if wlname == "cfg1" else [(65536, 64), (16384, 64)]
+        wl.name = wlname
+        cfg = C2CWorkload.config(wl)
+        sample = lambda rows, th: C2CWorkload.cpu_sample(wl, O, rows, th)
+    cores = os.cpu_count() or 1
+    rows = 256
+    for _ in range(max(1, min(args.warmup, 2))):
+        sample(rows, cores)
+    done = 0
+    t = 0.0
+    for _ in range(args.steps):
+        d, dt = sample(rows, cores)
+        done += d
+        t += dt
+    value = done / t / 1e9
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
+            "impl": "reference", "config": cfg,
+            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                             "sample": f"{rows} rows per transform length per step"},
+            "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,77 @@
+/*
+ * aclfft_ext.h - GB300 extensions to the aclfft C API.
+ *
+ * Everything here is new relative to the reference (which has no adjoints,
+ * no configurable normalisation, no precision modes and no plan
+ * introspection); the reference-compatible surface is cann_ops_fft.h.
+ */
+#ifndef ACLFFT_EXT_H
+#define ACLFFT_EXT_H
+
+#include "cann_ops_fft.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Normalisation.  The reference fixes normMode = 0 (lib/fft_handle_impl.h:36):
+ * neither direction is scaled.  The other modes scale by the total number
+ * of points n of one transform (nx for 1D, nx*ny for 2D). */
+typedef enum aclfftNormMode_t {
+    ACLFFT_NORM_NONE = 0,     /* reference behaviour: no scaling */
+    ACLFFT_NORM_BACKWARD = 1, /* backward (and C2R) scaled by 1/n */
+    ACLFFT_NORM_ORTHO = 2,    /* both directions scaled by 1/sqrt(n) */
+    ACLFFT_NORM_FORWARD = 3   /* forward (and R2C) scaled by 1/n */
+} aclfftNormMode;
+
+/* Sets the plan's normalisation (before or after MakePlan).  Returns
+ * ACLFFT_INVALID_VALUE for an unknown mode, ACLFFT_INVALID_PLAN for NULL. */
+ACLFFT_API aclfftResult aclfftSetNormMode(aclfftHandle plan, int normMode);
+ACLFFT_API aclfftResult aclfftGetNormMode(aclfftHandle plan, int* normMode);
+
+/* Adjoint (vector-Jacobian) transforms, using the complex-gradient convention
+ * g = dL/dRe + i dL/dIm.  Same pointer and stream semantics as the Exec
+ * calls; the plan's normalisation scale carries over unchanged.
+ *   C2C: the adjoint of direction d is the transform of direction -d.
+ *   R2C: gradIn[n] = Re sum_{k<=N/2} gradOut[k] exp(+2 pi i k n / N), i.e. a
+ *        C2R of gradOut with interior bins halved.
+ *   C2R: gradIn[k] = w_k * R2C(gradOut)[k], w = 1 at DC and Nyquist, 2 on
+ *        interior bins. */
+ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftComplex* gradIn,
+                                             int direction);
+ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftReal* gradIn);
+ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn);
+
+/* Plan introspection (for tests and tooling). */
+typedef struct aclfftPlanInfo_t {
+    int supported;        /* 1 when the plan can execute on the GPU */
+    int nsteps;           /* kernel launches per out-of-place exec */
+    int nradix;           /* passes of the first on-chip transform */
+    int radix[12];        /* their radices */
+    int onchip_length;    /* length of the first on-chip transform */
+    int threads_per_transform;
+    int transforms_per_cta;
+    long long twiddle_entries; /* complex entries generated on the GPU */
+    size_t workspace_bytes;    /* device workspace owned by the plan */
+} aclfftPlanInfo;
+
+ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info);
+
+/* Copies the plan's FP32 twiddle blob (as generated on the GPU) to host
+ * memory: at most maxEntries complex values; *entries receives the total. */
+ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host, long long maxEntries,
+                                          long long* entries);
+
+/* Replays the address arithmetic of every launch the plan can make against
+ * the buffer sizes of each call variant (no kernel runs).  Returns 0 when
+ * all launches stay in bounds; msg receives a description. */
+ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int msglen);
+
+/* Human-readable reason of the last failure on this thread ("" if none). */
+ACLFFT_API const char* aclfftGetLastErrorDetail(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACLFFT_EXT_H */

@@ -1,0 +1,248 @@
+"""ctypes binding of libops_fft.so (the GB300 aclfft C API).
+
+This is the Python face of the same C ABI a C/C++ caller links against:
+every call goes through ``libops_fft.so``; nothing here computes a
+transform.  Loading fails loudly when the library has not been built.
+
+    import aclfft
+    p = aclfft.Plan.plan1d(4096, aclfft.C2C, batch=256)
+    p.exec_c2c(x.data_ptr(), y.data_ptr(), aclfft.FORWARD)   # device tensors
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libops_fft.so")
+
+# include/cann_ops_fft.h
+SUCCESS = 0
+INVALID_PLAN = 1
+ALLOC_FAILED = 2
+INVALID_TYPE = 3
+INVALID_VALUE = 4
+INTERNAL_ERROR = 5
+EXEC_FAILED = 6
+SETUP_FAILED = 7
+INVALID_SIZE = 8
+UNALIGNED_DATA = 9
+INCOMPLETE_PARAMETER_LIST = 10
+INVALID_DEVICE = 11
+PARSE_ERROR = 12
+NO_WORKSPACE = 13
+NOT_IMPLEMENTED = 14
+NOT_SUPPORTED = 16
+
+R2C = 0x2A
+C2R = 0x2C
+C2C = 0x29
+D2Z = 0x6A
+Z2D = 0x6C
+Z2Z = 0x69
+
+FORWARD = -1
+BACKWARD = 1
+HORIZONTAL = 0
+VERTICAL = 1
+
+# include/aclfft_ext.h
+NORM_NONE = 0
+NORM_BACKWARD = 1
+NORM_ORTHO = 2
+NORM_FORWARD = 3
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [
+        ("supported", ctypes.c_int),
+        ("nsteps", ctypes.c_int),
+        ("nradix", ctypes.c_int),
+        ("radix", ctypes.c_int * 12),
+        ("onchip_length", ctypes.c_int),
+        ("threads_per_transform", ctypes.c_int),
+        ("transforms_per_cta", ctypes.c_int),
+        ("twiddle_entries", ctypes.c_longlong),
+        ("workspace_bytes", ctypes.c_size_t),
+    ]
+
+
+class AclfftError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        super().__init__(f"{what} failed with {code} ({error_string(code)}) {last_error_detail()}")
+
+
+_lib = None
+
+_H = ctypes.c_void_p
+_HP = ctypes.POINTER(ctypes.c_void_p)
+_I = ctypes.c_int
+_VP = ctypes.c_void_p
+_SZP = ctypes.POINTER(ctypes.c_size_t)
+
+_SIGNATURES = {
+    "aclfftPlan1d": [_HP, _I, _I, _I, _I],
+    "aclfftPlan2d": [_HP, _I, _I, _I, _I],
+    "aclfftPlan3d": [_HP, _I, _I, _I, _I],
+    "aclfftCreate": [_HP],
+    "aclfftMakePlan1d": [_H, _I, _I, _I, _I, _SZP],
+    "aclfftMakePlan2d": [_H, _I, _I, _I, _I, _SZP],
+    "aclfftMakePlan3d": [_H, _I, _I, _I, _I, _SZP],
+    "aclfftGetSize1d": [_H, _I, _I, _I, _SZP],
+    "aclfftGetSize2d": [_H, _I, _I, _I, _SZP],
+    "aclfftGetSize3d": [_H, _I, _I, _I, _I, _SZP],
+    "aclfftGetSize": [_H, _SZP],
+    "aclfftSetAutoAllocation": [_H, _I],
+    "aclfftSetWorkArea": [_H, _VP],
+    "aclfftExecC2C": [_H, _VP, _VP, _I],
+    "aclfftExecR2C": [_H, _VP, _VP],
+    "aclfftExecC2R": [_H, _VP, _VP],
+    "aclfftExecZ2Z": [_H, _VP, _VP, _I],
+    "aclfftExecD2Z": [_H, _VP, _VP],
+    "aclfftExecZ2D": [_H, _VP, _VP],
+    "aclfftSetStream": [_H, _VP],
+    "aclfftSetStride": [_H, ctypes.c_int32],
+    "aclfftDestroy": [_H],
+    "aclfftGetVersion": [ctypes.POINTER(_I)],
+    "aclfftGetProperty": [_I, ctypes.POINTER(_I)],
+    "aclfftSetNormMode": [_H, _I],
+    "aclfftGetNormMode": [_H, ctypes.POINTER(_I)],
+    "aclfftExecC2CAdjoint": [_H, _VP, _VP, _I],
+    "aclfftExecR2CAdjoint": [_H, _VP, _VP],
+    "aclfftExecC2RAdjoint": [_H, _VP, _VP],
+    "aclfftGetPlanInfo": [_H, ctypes.POINTER(PlanInfo)],
+    "aclfftGetTwiddles": [_H, _VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
+    "aclfftDebugCheckPlan": [_H, ctypes.c_char_p, _I],
+}
+
+
+def lib():
+    """Load libops_fft.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing: build it with ops-fft_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.aclfftGetErrorString.argtypes = [_I]
+        L.aclfftGetErrorString.restype = ctypes.c_char_p
+        L.aclfftGetLastErrorDetail.argtypes = []
+        L.aclfftGetLastErrorDetail.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def error_string(code: int) -> str:
+    return lib().aclfftGetErrorString(int(code)).decode()
+
+
+def last_error_detail() -> str:
+    return lib().aclfftGetLastErrorDetail().decode()
+
+
+def ptr(x) -> int:
+    """Address of a torch tensor, numpy array or raw integer pointer."""
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if hasattr(x, "ctypes"):
+        return int(x.ctypes.data)
+    raise TypeError(f"cannot take the address of {type(x)}")
+
+
+def _check(code: int, what: str):
+    if code != SUCCESS:
+        raise AclfftError(code, what)
+
+
+class Plan:
+    """Owning wrapper of an aclfftHandle."""
+
+    def __init__(self, handle: int):
+        self.handle = ctypes.c_void_p(handle)
+
+    @classmethod
+    def plan1d(cls, nx: int, type_: int, batch: int = 1, dim: int = HORIZONTAL) -> "Plan":
+        h = ctypes.c_void_p()
+        _check(lib().aclfftPlan1d(ctypes.byref(h), nx, type_, batch, dim), "aclfftPlan1d")
+        return cls(h.value)
+
+    @classmethod
+    def plan2d(cls, batch: int, nx: int, ny: int, type_: int = C2C) -> "Plan":
+        h = ctypes.c_void_p()
+        _check(lib().aclfftPlan2d(ctypes.byref(h), batch, nx, ny, type_), "aclfftPlan2d")
+        return cls(h.value)
+
+    def set_stream(self, stream) -> None:
+        s = getattr(stream, "cuda_stream", stream)
+        _check(lib().aclfftSetStream(self.handle, ctypes.c_void_p(int(s) if s else None)), "aclfftSetStream")
+
+    def set_norm(self, mode: int) -> None:
+        _check(lib().aclfftSetNormMode(self.handle, mode), "aclfftSetNormMode")
+
+    def exec_c2c(self, x, y, direction: int = FORWARD) -> None:
+        _check(lib().aclfftExecC2C(self.handle, ptr(x), ptr(y), direction), "aclfftExecC2C")
+
+    def exec_r2c(self, x, y) -> None:
+        _check(lib().aclfftExecR2C(self.handle, ptr(x), ptr(y)), "aclfftExecR2C")
+
+    def exec_c2r(self, x, y) -> None:
+        _check(lib().aclfftExecC2R(self.handle, ptr(x), ptr(y)), "aclfftExecC2R")
+
+    def exec_c2c_adjoint(self, g_out, g_in, direction: int = FORWARD) -> None:
+        _check(lib().aclfftExecC2CAdjoint(self.handle, ptr(g_out), ptr(g_in), direction), "aclfftExecC2CAdjoint")
+
+    def exec_r2c_adjoint(self, g_out, g_in) -> None:
+        _check(lib().aclfftExecR2CAdjoint(self.handle, ptr(g_out), ptr(g_in)), "aclfftExecR2CAdjoint")
+
+    def exec_c2r_adjoint(self, g_out, g_in) -> None:
+        _check(lib().aclfftExecC2RAdjoint(self.handle, ptr(g_out), ptr(g_in)), "aclfftExecC2RAdjoint")
+
+    def info(self) -> PlanInfo:
+        inf = PlanInfo()
+        _check(lib().aclfftGetPlanInfo(self.handle, ctypes.byref(inf)), "aclfftGetPlanInfo")
+        return inf
+
+    def twiddles(self):
+        import numpy as np
+
+        n = ctypes.c_longlong()
+        _check(lib().aclfftGetTwiddles(self.handle, None, 0, ctypes.byref(n)), "aclfftGetTwiddles")
+        out = np.zeros(n.value, dtype=np.complex64)
+        _check(lib().aclfftGetTwiddles(self.handle, out.ctypes.data, n.value, ctypes.byref(n)), "aclfftGetTwiddles")
+        return out
+
+    def check(self) -> str:
+        """Host-side bounds check of every launch of the plan ('ok' or why)."""
+        buf = ctypes.create_string_buffer(256)
+        rc = lib().aclfftDebugCheckPlan(self.handle, buf, 256)
+        msg = buf.value.decode()
+        if rc != 0:
+            raise AssertionError(msg)
+        return msg
+
+    def destroy(self) -> None:
+        if self.handle and self.handle.value:
+            lib().aclfftDestroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()

@@ -1,0 +1,282 @@
+// butterfly.cuh - in-register DFT butterflies for the Stockham kernels.
+//
+// DFT<R>::run(v) replaces v[0..R) by its forward (exp(-2*pi*i*k*n/R)) DFT in
+// natural order.  Every twiddle inside a butterfly is a compile-time constant
+// computed by our own constexpr sin/cos (a Taylor series in double after an
+// exact integer octant reduction), so the generated code holds immediates
+// only.  Backward transforms reuse the forward butterflies through
+// conj(DFT(conj(x))), applied by the kernels at load and store.
+//
+// Radix families:
+//   2, 3, 4, 5, 7          hand-derived minimal-operation forms
+//   odd primes p (11..47)  symmetric-pair form: for k = 1..(p-1)/2,
+//                          X_k, X_{p-k} = x0 + sum_j c_jk A_j -/+ i sum_j s_jk B_j
+//                          with A_j = x_j + x_{p-j}, B_j = x_j - x_{p-j}
+//   composite R = A*B      one decimation-in-time split (A-point over B-point)
+//                          with constant inter-stage twiddles W_R^{a*k1}
+#pragma once
+#include <cuda_runtime.h>
+#include <type_traits>
+#include <utility>
+
+#ifndef GFFT_HD
+#define GFFT_HD __host__ __device__ __forceinline__
+#endif
+
+namespace gfft {
+
+// ----------------------------------------------------------- static loops
+template <class F, int... Is>
+GFFT_HD void sfor_impl(F&& f, std::integer_sequence<int, Is...>)
+{
+    (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F>
+GFFT_HD void sfor(F&& f)
+{
+    sfor_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// ------------------------------------------------- compile-time unit roots
+constexpr double kPi = 3.14159265358979323846264338327950288;
+
+__host__ __device__ constexpr double taylor_sin(double x)
+{
+    double term = x, sum = x;
+    const double x2 = x * x;
+    for (int k = 1; k < 16; ++k) {
+        term *= -x2 / double((2 * k) * (2 * k + 1));
+        sum += term;
+    }
+    return sum;
+}
+__host__ __device__ constexpr double taylor_cos(double x)
+{
+    double term = 1.0, sum = 1.0;
+    const double x2 = x * x;
+    for (int k = 1; k < 16; ++k) {
+        term *= -x2 / double((2 * k - 1) * (2 * k));
+        sum += term;
+    }
+    return sum;
+}
+
+struct Root {
+    double c, s;  // cos and sin of the positive angle 2*pi*num/den
+};
+
+// cos/sin of 2*pi*num/den with the angle reduced exactly to one octant.
+__host__ __device__ constexpr Root unit_root(long long num, long long den)
+{
+    long long m = num % den;
+    if (m < 0) m += den;
+    const long long e = 8 * m;
+    const int oct = int(e / den);
+    const long long rem = e - (long long)oct * den;
+    const double a = double(rem) / double(den) * (kPi / 4.0);
+    const double ca = taylor_cos(a), sa = taylor_sin(a);
+    const double cb = taylor_cos(kPi / 4.0 - a), sb = taylor_sin(kPi / 4.0 - a);
+    switch (oct & 7) {
+    case 0: return {ca, sa};
+    case 1: return {sb, cb};
+    case 2: return {-sa, ca};
+    case 3: return {-cb, sb};
+    case 4: return {-ca, -sa};
+    case 5: return {-sb, -cb};
+    case 6: return {sa, -ca};
+    default: return {cb, -sb};
+    }
+}
+
+// Forward twiddle W_R^E = exp(-2*pi*i*E/R) as float components.
+template <int R, int E>
+struct W {
+    static constexpr Root r = unit_root(E, R);
+    static constexpr float re = float(r.c);
+    static constexpr float im = float(-r.s);
+};
+
+// ------------------------------------------------------ complex helpers
+GFFT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+GFFT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+GFFT_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+GFFT_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+GFFT_HD float2 cmul(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+GFFT_HD float2 cmulc(float2 a, float2 b)
+{
+    return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+GFFT_HD float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // * (-i)
+GFFT_HD float2 mul_pi(float2 a) { return make_float2(-a.y, a.x); }  // * (+i)
+
+// x * W_R^E with the trivial angles folded at compile time.
+template <int R, int E>
+GFFT_HD float2 twc(float2 x)
+{
+    constexpr int e = ((E % R) + R) % R;
+    if constexpr (e == 0) {
+        return x;
+    } else if constexpr (2 * e == R) {
+        return make_float2(-x.x, -x.y);
+    } else if constexpr (4 * e == R) {
+        return mul_mi(x);
+    } else if constexpr (4 * e == 3 * R) {
+        return mul_pi(x);
+    } else if constexpr (8 * e == R) {
+        constexpr float h = W<8, 1>::re;  // sqrt(1/2)
+        return make_float2((x.x + x.y) * h, (x.y - x.x) * h);
+    } else if constexpr (8 * e == 3 * R) {
+        constexpr float h = W<8, 1>::re;
+        return make_float2((x.y - x.x) * h, -(x.x + x.y) * h);
+    } else if constexpr (8 * e == 5 * R) {
+        constexpr float h = W<8, 1>::re;
+        return make_float2(-(x.x + x.y) * h, (x.x - x.y) * h);
+    } else if constexpr (8 * e == 7 * R) {
+        constexpr float h = W<8, 1>::re;
+        return make_float2((x.x - x.y) * h, (x.x + x.y) * h);
+    } else {
+        constexpr float c = W<R, e>::re, s = W<R, e>::im;
+        return make_float2(fmaf(x.x, c, -x.y * s), fmaf(x.x, s, x.y * c));
+    }
+}
+
+// --------------------------------------------------------- radix tables
+__host__ __device__ constexpr int smallest_factor(int n)
+{
+    if (n % 4 == 0 && n > 4) return 4;
+    for (int f = 2; f * f <= n; ++f)
+        if (n % f == 0) return f;
+    return n;
+}
+__host__ __device__ constexpr bool is_prime(int n)
+{
+    if (n < 2) return false;
+    for (int f = 2; f * f <= n; ++f)
+        if (n % f == 0) return false;
+    return true;
+}
+
+template <int R, class Enable = void>
+struct DFT;
+
+template <>
+struct DFT<1> {
+    GFFT_HD static void run(float2*) {}
+};
+
+template <>
+struct DFT<2> {
+    GFFT_HD static void run(float2* v)
+    {
+        const float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+
+template <>
+struct DFT<3> {
+    GFFT_HD static void run(float2* v)
+    {
+        constexpr float s3 = float(0.86602540378443864676372317075294);  // sin(2pi/3)
+        const float2 t1 = cadd(v[1], v[2]);
+        const float2 t2 = make_float2(fmaf(-0.5f, t1.x, v[0].x), fmaf(-0.5f, t1.y, v[0].y));
+        const float2 d = csub(v[1], v[2]);
+        const float2 t3 = make_float2(s3 * d.y, -s3 * d.x);  // -i*s3*(v1-v2)
+        v[0] = cadd(v[0], t1);
+        v[1] = cadd(t2, t3);
+        v[2] = csub(t2, t3);
+    }
+};
+
+template <>
+struct DFT<4> {
+    GFFT_HD static void run(float2* v)
+    {
+        const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        const float2 c = cadd(v[1], v[3]), d = mul_mi(csub(v[1], v[3]));
+        v[0] = cadd(a, c);
+        v[2] = csub(a, c);
+        v[1] = cadd(b, d);
+        v[3] = csub(b, d);
+    }
+};
+
+// Odd primes >= 5: symmetric-pair evaluation.
+template <int P>
+struct DFT<P, std::enable_if_t<(P >= 5) && is_prime(P)>> {
+    GFFT_HD static void run(float2* v)
+    {
+        constexpr int H = (P - 1) / 2;
+        float2 A[H], B[H];
+        float2 sum = v[0];
+        sfor<H>([&](auto jj) {
+            constexpr int j = decltype(jj)::value + 1;
+            A[j - 1] = cadd(v[j], v[P - j]);
+            B[j - 1] = csub(v[j], v[P - j]);
+            sum = cadd(sum, A[j - 1]);
+        });
+        const float2 x0 = v[0];
+        v[0] = sum;
+        sfor<H>([&](auto kk) {
+            constexpr int k = decltype(kk)::value + 1;
+            float2 re = x0;                       // x0 + sum c*A
+            float2 im = make_float2(0.f, 0.f);    // sum s*B
+            sfor<H>([&](auto jj) {
+                constexpr int j = decltype(jj)::value + 1;
+                constexpr Root rt = unit_root((long long)j * k, P);
+                constexpr float c = float(rt.c), s = float(rt.s);
+                re.x = fmaf(c, A[j - 1].x, re.x);
+                re.y = fmaf(c, A[j - 1].y, re.y);
+                im.x = fmaf(s, B[j - 1].x, im.x);
+                im.y = fmaf(s, B[j - 1].y, im.y);
+            });
+            // X_k = re - i*im ; X_{P-k} = re + i*im
+            v[k] = make_float2(re.x + im.y, re.y - im.x);
+            v[P - k] = make_float2(re.x - im.y, re.y + im.x);
+        });
+    }
+};
+
+// Composite radices: R = A * B, decimation in time.
+template <int R>
+struct DFT<R, std::enable_if_t<(R > 4) && !is_prime(R)>> {
+    static constexpr int A = smallest_factor(R);
+    static constexpr int B = R / A;
+    GFFT_HD static void run(float2* v)
+    {
+        float2 t[R];
+        sfor<A>([&](auto aa) {
+            constexpr int a = decltype(aa)::value;
+            float2 u[B];
+            sfor<B>([&](auto mm) {
+                constexpr int m = decltype(mm)::value;
+                u[m] = v[a + A * m];
+            });
+            DFT<B>::run(u);
+            sfor<B>([&](auto kk) {
+                constexpr int k1 = decltype(kk)::value;
+                t[a * B + k1] = twc<R, a * k1>(u[k1]);
+            });
+        });
+        sfor<B>([&](auto kk) {
+            constexpr int k1 = decltype(kk)::value;
+            float2 w[A];
+            sfor<A>([&](auto aa) {
+                constexpr int a = decltype(aa)::value;
+                w[a] = t[a * B + k1];
+            });
+            DFT<A>::run(w);
+            sfor<A>([&](auto qq) {
+                constexpr int k2 = decltype(qq)::value;
+                v[k1 + B * k2] = w[k2];
+            });
+        });
+    }
+};
+
+}  // namespace gfft

@@ -1,0 +1,134 @@
+// kernel_args.h - argument blocks shared by the host planner (lib/) and the
+// CUDA kernels (csrc/).  Plain C++ with fixed-width fields only, so the host
+// side compiles without CUDA headers.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+namespace gfft {
+
+constexpr int kMaxPass = 12;        // on-chip Stockham passes per transform
+constexpr int kMaxSmemBytes = 227 * 1024;
+
+// One on-chip Stockham pass: radix R after a product `ns` of earlier radices.
+// Butterfly j reads x[j + r*L/R] and writes y[(j/ns)*ns*R + j%ns + r*ns]
+// after multiplying input r by W_{ns*R}^{(j%ns)*r} (table at tw_off, rows of
+// R entries, one row per j%ns).
+struct PassDesc {
+    int32_t radix;
+    int32_t ns;
+    uint32_t ns_magic;  // ceil(2^32/ns): j/ns == umulhi(j, magic) for j, ns < 2^16
+    int32_t tw_off;     // float2 offset of this pass's table, -1 when ns == 1
+};
+
+// How the on-chip transform of length L is executed.
+struct InnerPlan {
+    int32_t L;
+    int32_t npass;
+    int32_t rmax;   // largest radix, selects the kernel instantiation (16 or 47)
+    int32_t nthr;   // threads cooperating on one transform
+    PassDesc pass[kMaxPass];
+};
+
+enum IoMode : int32_t {
+    IO_C2C = 0,       // complex in, complex out
+    IO_R2C_EVEN = 1,  // real in viewed as L=N/2 complex, fused even/odd post-process
+    IO_C2R_EVEN = 2,  // N/2+1 bins in, fused pre-process, real out viewed as complex
+    IO_R2C_ODD = 3,   // real in, full N-point transform, first N/2+1 bins out
+    IO_C2R_ODD = 4,   // Hermitian-expanded load, full N-point transform, real part out
+};
+
+enum WeightMode : int32_t {
+    WEIGHT_NONE = 0,
+    WEIGHT_STORE_X2 = 1,   // multiply interior output bins by 2 (C2R adjoint)
+    WEIGHT_LOAD_HALF = 2,  // multiply interior input bins by 1/2 (R2C adjoint)
+};
+
+// Contiguous transforms, one on-chip transform per batch item.
+struct RowArgs {
+    InnerPlan ip;
+    const void* tw;       // float2 pass tables
+    const void* post_tw;  // float2 W_N^k for k <= L/2 (even R2C/C2R), N = 2L
+    const void* in;
+    void* out;
+    int64_t ntf;       // number of transforms
+    int64_t in_dist;   // distance between transforms, in elements of the input type
+    int64_t out_dist;  // same for the output
+    int32_t tfpc;      // transforms per CTA
+    int32_t lpad;      // float2 pitch of one shared buffer
+    int32_t nbuf;      // shared buffers per transform (1 or 2)
+    int32_t io_mode;
+    int32_t conj_in;   // conjugate on load (backward transforms)
+    int32_t conj_out;  // conjugate on store
+    int32_t weight;
+    int32_t nreal;     // N for the real-data modes
+    int32_t staged;    // cooperative contiguous copies through shared memory
+    float scale;
+};
+
+// Strided ("column") transforms, optionally one outer Stockham pass of a
+// longer transform.  Column c (0 <= c < ncols) belongs to item c / cpi and
+// has local index j = c % cpi; element r of it is read from
+//   in  + item*in_dist  + (j / in_split)*in_hi  + (j % in_split)*in_lo  + r*in_stride
+// and output bin k is written to
+//   out + item*out_dist + (j / out_split)*out_hi + (j % out_split)*out_lo + k*out_stride
+// (float2 units).  When ons > 1, input r is first multiplied by
+// W_{ons*L}^{((j / tw_div) % ons) * r}, read as hi[m >> otw_shift] * lo[m & mask].
+struct ColArgs {
+    InnerPlan ip;
+    const void* tw;
+    const void* otw_hi;
+    const void* otw_lo;
+    const void* in;
+    void* out;
+    int64_t ncols;
+    int64_t cpi;
+    int64_t in_dist, in_split, in_hi, in_lo, in_stride;
+    int64_t out_dist, out_split, out_hi, out_lo, out_stride;
+    int64_t ons;
+    int64_t tw_div;
+    int32_t otw_shift;
+    int32_t tfpc;      // columns per CTA
+    int32_t tfp;       // shared-memory pitch in columns (>= tfpc)
+    int32_t nbuf;      // shared buffers (1 or 2), each L*tfp float2
+    int32_t conj_in;
+    int32_t conj_out;
+    int32_t staged_out;  // output of column c is out + c*L + k (contiguous blocks)
+    float scale;
+};
+
+// Stand-alone even/odd packing for R2C/C2R lengths beyond one CTA.
+struct PackArgs {
+    const void* in;
+    void* out;
+    const void* post_tw;  // W_N^k, k <= L/2
+    int64_t ntf;
+    int64_t in_dist, out_dist;  // float2 units
+    int32_t L;                  // N/2
+    int32_t c2r;                // 0: Z -> X (R2C post), 1: X -> conj(Z') (C2R pre)
+    int32_t weight;
+    float scale;
+};
+
+// Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
+//   kind 0: f(i) = ((i / R) * (i % R)) mod M      (pass tables, rows of R)
+//   kind 1: f(i) = (i * mult) mod M               (linear tables)
+struct TwSeg {
+    int64_t offset;  // float2 offset in the table blob
+    int64_t count;
+    int64_t M;
+    int64_t R_or_mult;
+    int32_t kind;
+    int32_t pad_;
+};
+
+}  // namespace gfft
+
+// Launchers exported by the CUDA translation units (C linkage, plain types).
+extern "C" {
+int gfft_launch_row(const gfft::RowArgs* a, void* stream);
+int gfft_launch_col(const gfft::ColArgs* a, void* stream);
+int gfft_launch_pack(const gfft::PackArgs* a, void* stream);
+int gfft_gen_twiddles(void* table, const gfft::TwSeg* segs, int nseg, void* stream);
+int gfft_kernel_max_threads(int rmax);
+}

@@ -1,0 +1,61 @@
+// launch_common.cuh - host-side launch helpers for the Stockham kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "stockham.cuh"
+
+namespace gfft {
+
+// Opt a kernel into >48 KB of dynamic shared memory once per device.
+template <class K>
+inline cudaError_t ensure_smem_attr(K kernel, unsigned long long& done_mask, size_t bytes)
+{
+    if (bytes <= 48 * 1024) return cudaSuccess;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done_mask & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemBytes);
+    if (e == cudaSuccess) done_mask |= bit;
+    return e;
+}
+
+template <int RMAX>
+int launch_row_t(const RowArgs* a, cudaStream_t st)
+{
+    static unsigned long long attr_mask = 0;
+    const int threads = a->ip.nthr * a->tfpc;
+    if (threads <= 0 || threads > kernel_max_threads<RMAX>() || a->ntf <= 0) return (int)cudaErrorInvalidValue;
+    const size_t smem = (size_t)a->tfpc * (size_t)a->nbuf * (size_t)a->lpad * sizeof(float2);
+    if (smem > (size_t)kMaxSmemBytes) return (int)cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(row_kernel<RMAX>, attr_mask, smem);
+    if (e != cudaSuccess) return (int)e;
+    const int64_t grid = (a->ntf + a->tfpc - 1) / a->tfpc;
+    if (grid > 0x7fffffff) return (int)cudaErrorInvalidValue;
+    row_kernel<RMAX><<<(unsigned)grid, threads, smem, st>>>(*a);
+    return (int)cudaGetLastError();
+}
+
+template <int RMAX>
+int launch_col_t(const ColArgs* a, cudaStream_t st)
+{
+    static unsigned long long attr_mask = 0;
+    const int threads = a->ip.nthr * a->tfpc;
+    if (threads <= 0 || threads > kernel_max_threads<RMAX>() || a->ncols <= 0) return (int)cudaErrorInvalidValue;
+    const size_t smem = (size_t)a->nbuf * (size_t)a->ip.L * (size_t)a->tfp * sizeof(float2);
+    if (smem > (size_t)kMaxSmemBytes) return (int)cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(col_kernel<RMAX>, attr_mask, smem);
+    if (e != cudaSuccess) return (int)e;
+    const int64_t grid = (a->ncols + a->tfpc - 1) / a->tfpc;
+    if (grid > 0x7fffffff) return (int)cudaErrorInvalidValue;
+    col_kernel<RMAX><<<(unsigned)grid, threads, smem, st>>>(*a);
+    return (int)cudaGetLastError();
+}
+
+int launch_row_r16(const RowArgs* a, cudaStream_t st);
+int launch_row_r47(const RowArgs* a, cudaStream_t st);
+int launch_col_r16(const ColArgs* a, cudaStream_t st);
+int launch_col_r47(const ColArgs* a, cudaStream_t st);
+
+}  // namespace gfft

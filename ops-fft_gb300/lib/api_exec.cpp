@@ -1,0 +1,296 @@
+// api_exec.cpp - transform execution.
+//
+// Entry checks mirror lib/fft_exec_api.cpp:32-85 of the reference (plan
+// initialised, non-NULL buffers, matching plan type, valid direction) and the
+// 1D op-layer checks of src/common/host/fft_exec_helper.h:37-47 (R2C/C2R
+// reject VERTICAL plans with ACLFFT_NOT_IMPLEMENTED).  Lengths outside the
+// supported domain (a prime factor > 47) also return ACLFFT_NOT_IMPLEMENTED,
+// like the reference's dispatchers (src/fft1_d/arch35/fft1_d_exec_api.cpp:
+// 42-74).  Device failures map to ACLFFT_EXEC_FAILED as in
+// src/fft1_d/arch32/fft1_d_exec_api.cpp:148-152.
+//
+// Pointer semantics: device/managed pointers run asynchronously on the
+// plan's stream (capturable in CUDA graphs); host pointers are staged
+// through plan-owned device buffers and the call synchronises the stream
+// before returning, which is the reference's contract for host buffers.
+#include <cmath>
+#include <thread>
+
+#include "handle.h"
+
+using gfft::PlanImpl;
+using gfft::Step;
+using gfft::StepList;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+bool device_accessible(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+double points(const aclfftHandle_t* h)
+{
+    return h->rank == 2 ? (double)h->lengths[0] * (double)h->lengths[1] : (double)h->lengths[0];
+}
+
+float norm_scale(const aclfftHandle_t* h, bool backward_like)
+{
+    const double n = points(h);
+    switch (h->normMode) {
+    case ACLFFT_NORM_BACKWARD: return backward_like ? (float)(1.0 / n) : 1.f;
+    case ACLFFT_NORM_ORTHO: return (float)(1.0 / std::sqrt(n));
+    case ACLFFT_NORM_FORWARD: return backward_like ? 1.f : (float)(1.0 / n);
+    default: return 1.f;
+    }
+}
+
+int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStream_t st, bool c2c, bool inverse,
+                float scale)
+{
+    void* bufs[4] = {in, out, impl->ws, impl->ws2};
+    const float2* tw = static_cast<const float2*>(impl->tw);
+    const size_t n = sl.steps.size();
+    for (size_t i = 0; i < n; ++i) {
+        Step s = sl.steps[i];
+        const bool first = i == 0, last = i + 1 == n;
+        void* src = bufs[s.src];
+        void* dst = bufs[s.dst];
+        int rc = 0;
+        switch (s.kind) {
+        case Step::ROW:
+            s.row.tw = tw;
+            s.row.post_tw = s.post_off >= 0 ? tw + s.post_off : nullptr;
+            s.row.in = src;
+            s.row.out = dst;
+            if (c2c) {
+                s.row.conj_in = first && inverse;
+                s.row.conj_out = last && inverse;
+            }
+            if (last) s.row.scale = scale;
+            rc = gfft_launch_row(&s.row, st);
+            break;
+        case Step::COL:
+            s.col.tw = tw;
+            s.col.otw_hi = s.hi_off >= 0 ? tw + s.hi_off : nullptr;
+            s.col.otw_lo = s.lo_off >= 0 ? tw + s.lo_off : nullptr;
+            s.col.in = src;
+            s.col.out = dst;
+            if (c2c) {
+                s.col.conj_in = first && inverse;
+                s.col.conj_out = last && inverse;
+            }
+            if (last) s.col.scale = scale;
+            rc = gfft_launch_col(&s.col, st);
+            break;
+        case Step::PACK:
+            s.pack.post_tw = tw + s.post_off;
+            s.pack.in = src;
+            s.pack.out = dst;
+            if (last) s.pack.scale = scale;
+            rc = gfft_launch_pack(&s.pack, st);
+            break;
+        case Step::COPY:
+            rc = (int)cudaMemcpyAsync(dst, src, (size_t)s.copy_bytes, cudaMemcpyDeviceToDevice, st);
+            break;
+        }
+        if (rc != 0) {
+            gfft::set_last_error(std::string("kernel launch failed: ") + cudaGetErrorString((cudaError_t)rc));
+            cudaGetLastError();
+            return rc;
+        }
+    }
+    return 0;
+}
+
+struct CallShape {
+    size_t in_bytes;
+    size_t out_bytes;
+};
+
+// variant 0 = primary transform, 2 = adjoint transform
+aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, CallShape shape, bool c2c,
+                         bool inverse, bool backward_like)
+{
+    PlanImpl* impl = h->impl;
+    if (!impl) return ACLFFT_INTERNAL_ERROR;
+    const StepList& primary = impl->lists[variant];
+    if (!primary.supported) {
+        GFFT_LOG("exec: %s", primary.why.c_str());
+        gfft::set_last_error(primary.why);
+        return ACLFFT_NOT_IMPLEMENTED;
+    }
+    if (!impl->device_ready) {
+        if (gfft::plan_device_setup(impl) != ACLFFT_SUCCESS || !impl->device_ready) {
+            gfft::set_last_error("no usable CUDA device");
+            return ACLFFT_EXEC_FAILED;
+        }
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    if (dev != impl->device) {
+        gfft::set_last_error("plan executed on a different device than it was created on");
+        return ACLFFT_INVALID_DEVICE;
+    }
+    const float scale = norm_scale(h, backward_like);
+    cudaStream_t st = h->stream;
+    const bool din = device_accessible(in), dout = device_accessible(out);
+    if (din && dout) {
+        const StepList& sl = (in == out) ? impl->lists[variant + 1] : primary;
+        if (!sl.supported) return ACLFFT_NOT_IMPLEMENTED;
+        return launch_list(impl, sl, in, out, st, c2c, inverse, scale) == 0 ? ACLFFT_SUCCESS : ACLFFT_EXEC_FAILED;
+    }
+    // host buffers: stage through device memory, return when done
+    const size_t need = std::max(shape.in_bytes, shape.out_bytes);
+    if (impl->stage_bytes < need) {
+        if (impl->stage_a) cudaFree(impl->stage_a);
+        if (impl->stage_b) cudaFree(impl->stage_b);
+        impl->stage_a = impl->stage_b = nullptr;
+        impl->stage_bytes = 0;
+        if (cudaMalloc(&impl->stage_a, need) != cudaSuccess || cudaMalloc(&impl->stage_b, need) != cudaSuccess) {
+            cudaGetLastError();
+            if (impl->stage_a) cudaFree(impl->stage_a);
+            impl->stage_a = impl->stage_b = nullptr;
+            gfft::set_last_error("cudaMalloc of the host staging buffers failed");
+            return ACLFFT_EXEC_FAILED;
+        }
+        impl->stage_bytes = need;
+    }
+    void* dev_in = din ? in : impl->stage_a;
+    void* dev_out = dout ? out : impl->stage_b;
+    if (!din && cudaMemcpyAsync(dev_in, in, shape.in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    const StepList& sl = (dev_in == dev_out) ? impl->lists[variant + 1] : primary;
+    if (launch_list(impl, sl, dev_in, dev_out, st, c2c, inverse, scale) != 0) {
+        cudaStreamSynchronize(st);
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    if (!dout && cudaMemcpyAsync(out, dev_out, shape.out_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    return ACLFFT_SUCCESS;
+}
+
+size_t complex_elems(const aclfftHandle_t* h)
+{
+    if (h->rank == 2) return (size_t)h->batch * h->lengths[0] * h->lengths[1];
+    return (size_t)h->batch * (size_t)h->lengths[0] * (size_t)(h->stride[0] > 1 ? h->stride[0] : 1);
+}
+
+size_t real_elems(const aclfftHandle_t* h) { return (size_t)h->batch * (size_t)h->lengths[0]; }
+size_t half_elems(const aclfftHandle_t* h) { return (size_t)h->batch * (size_t)(h->lengths[0] / 2 + 1); }
+
+#define EXEC_PLAN_CHECKS(plan, a, b, expected)                                \
+    ACLFFT_CHECK_NULL(plan);                                                  \
+    ACLFFT_CHECK_PARAM((plan)->is_initialized, ACLFFT_INVALID_PLAN);          \
+    ACLFFT_CHECK_NULL(a);                                                     \
+    ACLFFT_CHECK_NULL(b);                                                     \
+    ACLFFT_CHECK_PARAM((plan)->type == (expected), ACLFFT_INVALID_TYPE)
+
+}  // namespace
+
+namespace gfft {
+void set_last_error(const std::string& s) { g_last_error = s; }
+}  // namespace gfft
+
+extern "C" {
+
+ACLFFT_API aclfftResult aclfftExecC2C(aclfftHandle plan, aclfftComplex* idata, aclfftComplex* odata, int direction)
+{
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_C2C);
+    ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
+    if (plan->rank != 1 && plan->rank != 2) return ACLFFT_NOT_IMPLEMENTED;
+    const size_t bytes = complex_elems(plan) * 8;
+    const bool inv = direction == ACLFFT_BACKWARD;
+    return exec_common(plan, 0, idata, odata, {bytes, bytes}, true, inv, inv);
+}
+
+ACLFFT_API aclfftResult aclfftExecR2C(aclfftHandle plan, aclfftReal* idata, aclfftComplex* odata)
+{
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_R2C);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 0, idata, odata, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false, false);
+}
+
+ACLFFT_API aclfftResult aclfftExecC2R(aclfftHandle plan, aclfftComplex* idata, aclfftReal* odata)
+{
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_C2R);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 0, idata, odata, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false, true);
+}
+
+ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftComplex* gradIn,
+                                             int direction)
+{
+    EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_C2C);
+    ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
+    if (plan->rank != 1 && plan->rank != 2) return ACLFFT_NOT_IMPLEMENTED;
+    const size_t bytes = complex_elems(plan) * 8;
+    const bool primary_inv = direction == ACLFFT_BACKWARD;
+    // adjoint of direction d is direction -d with the primary's scale
+    return exec_common(plan, 0, gradOut, gradIn, {bytes, bytes}, true, !primary_inv, primary_inv);
+}
+
+ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftReal* gradIn)
+{
+    EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_R2C);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 2, gradOut, gradIn, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false,
+                       false);
+}
+
+ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn)
+{
+    EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_C2R);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 2, gradOut, gradIn, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false,
+                       true);
+}
+
+ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleComplex* odata,
+                                      int direction)
+{
+    (void)plan;
+    (void)idata;
+    (void)odata;
+    (void)direction;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata)
+{
+    (void)plan;
+    (void)idata;
+    (void)odata;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleReal* odata)
+{
+    (void)plan;
+    (void)idata;
+    (void)odata;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API const char* aclfftGetLastErrorDetail(void) { return g_last_error.c_str(); }
+
+}  // extern "C"

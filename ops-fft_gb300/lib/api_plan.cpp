@@ -1,0 +1,353 @@
+// api_plan.cpp - plan creation, initialisation, stream binding, destruction.
+//
+// Validation order and error codes follow the reference API layer:
+//   aclfftCreate       lib/fft_plan_api.cpp:24-36
+//   aclfftPlan1d       lib/fft_plan_api.cpp:47-85
+//   aclfftPlan2d       lib/fft_plan_api.cpp:90-122
+//   aclfftPlan3d       lib/fft_plan_api.cpp:127-150
+//   aclfftMakePlan1d   lib/fft_plan_init_api.cpp:118-176 (VERTICAL encodes
+//                      batch = 1, stride[0] = batch, :154-159)
+//   aclfftMakePlan2d   lib/fft_plan_init_api.cpp:189-236
+//   size domain        lib/fft_plan_validate.h:20-47
+//   overflow checks    lib/fft_plan_init_api.cpp:25-105
+//   aclfftSetStream    lib/fft_stream_api.cpp:22-32
+//   aclfftDestroy      lib/fft_plan_destroy_api.cpp:24-40
+// Deliberate differences: MakePlan also plans the GPU execution (radix
+// sequence, twiddles generated on the GPU, workspace), *workSize reports the
+// workspace the plan owns, and 2D plans accept any C2C size (the reference
+// only has {32,64,128}^2 kernels and returns ACLFFT_NOT_SUPPORTED otherwise).
+#include <cstring>
+#include <new>
+
+#include "handle.h"
+
+using gfft::Kind;
+using gfft::PlanImpl;
+using gfft::Problem;
+
+namespace {
+
+constexpr int kHorizontalMaxN = 1 << 27;
+constexpr int kVerticalMinN = 256;
+constexpr int kVerticalMaxN = 1 << 18;
+
+bool valid_type(aclfftType t)
+{
+    switch (t) {
+    case ACLFFT_C2C:
+    case ACLFFT_R2C:
+    case ACLFFT_C2R:
+    case ACLFFT_Z2Z:
+    case ACLFFT_D2Z:
+    case ACLFFT_Z2D:
+        return true;
+    default:
+        return false;
+    }
+}
+
+aclfftResult validate_1d_size(int dimType, int nx, const char* entry)
+{
+    if (dimType == ACLFFT_HORIZONTAL) {
+        if (nx > kHorizontalMaxN) {
+            GFFT_LOG("%s: nx=%d exceeds 2^27 for horizontal FFT", entry, nx);
+            return ACLFFT_INVALID_SIZE;
+        }
+    } else {
+        const bool pow2 = nx > 0 && (nx & (nx - 1)) == 0;
+        if (nx < kVerticalMinN || nx > kVerticalMaxN || !pow2) {
+            GFFT_LOG("%s: nx=%d out of [256, 262144] or not a power of 2 for vertical FFT", entry, nx);
+            return ACLFFT_INVALID_SIZE;
+        }
+    }
+    return ACLFFT_SUCCESS;
+}
+
+// Overflow-checked element counts of the plan's input and output.
+aclfftResult check_sizes(const aclfftHandle_t* p)
+{
+    size_t full = 1, packed = 1, tmp = 0;
+    for (int i = 0; i < p->rank; ++i)
+        if (__builtin_mul_overflow(full, (size_t)p->lengths[i], &full)) return ACLFFT_INVALID_SIZE;
+    if (__builtin_mul_overflow(full, (size_t)p->batch, &full)) return ACLFFT_INVALID_SIZE;
+    for (int i = 0; i < p->rank - 1; ++i)
+        if (__builtin_mul_overflow(packed, (size_t)p->lengths[i], &packed)) return ACLFFT_INVALID_SIZE;
+    if (__builtin_mul_overflow(packed, (size_t)(p->lengths[p->rank - 1] / 2 + 1), &packed) ||
+        __builtin_mul_overflow(packed, (size_t)p->batch, &packed))
+        return ACLFFT_INVALID_SIZE;
+    const size_t elem = (p->type == ACLFFT_Z2Z || p->type == ACLFFT_D2Z || p->type == ACLFFT_Z2D) ? 8 : 4;
+    if (__builtin_mul_overflow(full, (size_t)2 * elem, &tmp) || __builtin_mul_overflow(packed, (size_t)2 * elem, &tmp))
+        return ACLFFT_INVALID_SIZE;
+    return ACLFFT_SUCCESS;
+}
+
+// Plans every call variant of the transform described by the handle.
+aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
+{
+    PlanImpl* impl = new (std::nothrow) PlanImpl();
+    if (!impl) return ACLFFT_ALLOC_FAILED;
+    Problem pr;
+    pr.rank = h->rank;
+    pr.kind = h->type == ACLFFT_C2C ? Kind::C2C : (h->type == ACLFFT_R2C ? Kind::R2C : Kind::C2R);
+    pr.n0 = h->lengths[0];
+    pr.n1 = h->rank == 2 ? h->lengths[1] : 1;
+    pr.batch = h->batch;
+    pr.stride = h->rank == 1 ? h->stride[0] : 1;
+    impl->prob = pr;
+    Problem adj = pr;
+    if (pr.kind == Kind::R2C) {
+        adj.kind = Kind::C2R;
+        adj.weight = gfft::WEIGHT_LOAD_HALF;
+    } else if (pr.kind == Kind::C2R) {
+        adj.kind = Kind::R2C;
+        adj.weight = gfft::WEIGHT_STORE_X2;
+    }
+    bool ok = true;
+    for (int v = 0; v < 4 && ok; ++v) {
+        int64_t ws = 0, ws2 = 0;
+        ok = gfft::build_steps(v < 2 ? pr : adj, (v & 1) != 0, impl->tb, impl->lists[v], ws, ws2);
+        impl->ws_bytes = std::max<int64_t>(impl->ws_bytes, ws);
+        impl->ws2_bytes = std::max<int64_t>(impl->ws2_bytes, ws2);
+    }
+    if (!ok) {
+        delete impl;
+        gfft::set_last_error("internal planning failure");
+        return ACLFFT_INTERNAL_ERROR;
+    }
+    h->impl = impl;
+    const aclfftResult r = gfft::plan_device_setup(impl);
+    if (r != ACLFFT_SUCCESS) {
+        gfft::plan_impl_free(impl);
+        delete impl;
+        h->impl = nullptr;
+        return r;
+    }
+    if (workSize) *workSize = (size_t)(impl->ws_bytes + impl->ws2_bytes);
+    return ACLFFT_SUCCESS;
+}
+
+}  // namespace
+
+namespace gfft {
+
+void plan_impl_free(PlanImpl* p)
+{
+    if (!p) return;
+    if (p->tw) cudaFree(p->tw);
+    if (p->ws) cudaFree(p->ws);
+    if (p->ws2) cudaFree(p->ws2);
+    if (p->stage_a) cudaFree(p->stage_a);
+    if (p->stage_b) cudaFree(p->stage_b);
+    p->tw = p->ws = p->ws2 = p->stage_a = p->stage_b = nullptr;
+    p->device_ready = false;
+}
+
+// Allocates the twiddle blob and workspace on the current device and fills
+// the blob with the FP64-evaluated, FP32-rounded unit roots.  Without a CUDA
+// device the plan stays host-only and the setup is retried at exec time.
+aclfftResult plan_device_setup(PlanImpl* p)
+{
+    if (p->device_ready) return ACLFFT_SUCCESS;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return ACLFFT_SUCCESS;  // deferred
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_SETUP_FAILED;
+    }
+    const size_t tw_bytes = (size_t)std::max<int64_t>(p->tb.count, 2) * 8;
+    if (cudaMalloc(&p->tw, tw_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p->tw = nullptr;
+        set_last_error("cudaMalloc of the twiddle table failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    if (p->ws_bytes > 0 && cudaMalloc(&p->ws, (size_t)p->ws_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p->ws = nullptr;
+        plan_impl_free(p);
+        set_last_error("cudaMalloc of the workspace failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    if (p->ws2_bytes > 0 && cudaMalloc(&p->ws2, (size_t)p->ws2_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p->ws2 = nullptr;
+        plan_impl_free(p);
+        set_last_error("cudaMalloc of the second workspace failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    if (!p->tb.segs.empty()) {
+        const int rc = gfft_gen_twiddles(p->tw, p->tb.segs.data(), (int)p->tb.segs.size(), nullptr);
+        if (rc != 0 || cudaStreamSynchronize(nullptr) != cudaSuccess) {
+            cudaGetLastError();
+            plan_impl_free(p);
+            set_last_error("twiddle generation failed");
+            return ACLFFT_SETUP_FAILED;
+        }
+    }
+    p->device = dev;
+    p->device_ready = true;
+    return ACLFFT_SUCCESS;
+}
+
+}  // namespace gfft
+
+extern "C" {
+
+ACLFFT_API aclfftResult aclfftCreate(aclfftHandle* plan)
+{
+    ACLFFT_CHECK_NULL(plan);
+    aclfftHandle_t* p = new (std::nothrow) aclfftHandle_t();
+    if (!p) return ACLFFT_ALLOC_FAILED;
+    *plan = p;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftMakePlan1d(aclfftHandle plan, int nx, aclfftType type, int batch, int dimType,
+                                         size_t* workSize)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(!plan->is_initialized, ACLFFT_INVALID_VALUE);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(dimType == ACLFFT_HORIZONTAL || dimType == ACLFFT_VERTICAL, ACLFFT_INVALID_VALUE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
+        GFFT_LOG("aclfftMakePlan1d: type=%d has no 1D execution implementation yet", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
+    if (validate_1d_size(dimType, nx, "aclfftMakePlan1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    plan->rank = 1;
+    plan->lengths[0] = nx;
+    plan->batch = batch;
+    plan->type = type;
+    if (dimType == ACLFFT_VERTICAL) {
+        plan->batch = 1;
+        plan->stride[0] = batch;
+    } else {
+        plan->stride[0] = 1;
+    }
+    if (check_sizes(plan) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    const aclfftResult r = plan_execution(plan, workSize);
+    if (r != ACLFFT_SUCCESS) return r;
+    plan->is_initialized = true;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, int ny, aclfftType type,
+                                         size_t* workSize)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(!plan->is_initialized, ACLFFT_INVALID_VALUE);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) {
+        GFFT_LOG("aclfftMakePlan2d: type=%d has no 2D execution implementation yet", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
+    plan->rank = 2;
+    plan->lengths[0] = nx;
+    plan->lengths[1] = ny;
+    plan->batch = batch;
+    plan->type = type;
+    plan->stride[0] = 1;
+    plan->stride[1] = 1;
+    if (check_sizes(plan) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    const aclfftResult r = plan_execution(plan, workSize);
+    if (r != ACLFFT_SUCCESS) return r;
+    plan->is_initialized = true;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftMakePlan3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
+                                         size_t* workSize)
+{
+    (void)plan;
+    (void)nx;
+    (void)ny;
+    (void)nz;
+    (void)type;
+    (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftPlan1d(aclfftHandle* plan, int nx, aclfftType type, int batch, int dimType)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(dimType == ACLFFT_HORIZONTAL || dimType == ACLFFT_VERTICAL, ACLFFT_INVALID_VALUE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
+        GFFT_LOG("aclfftPlan1d: type=%d has no 1D execution implementation yet", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
+    if (validate_1d_size(dimType, nx, "aclfftPlan1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    aclfftResult r = aclfftCreate(plan);
+    if (r != ACLFFT_SUCCESS) return r;
+    r = aclfftMakePlan1d(*plan, nx, type, batch, dimType, nullptr);
+    if (r != ACLFFT_SUCCESS) {
+        aclfftDestroy(*plan);
+        *plan = nullptr;
+    }
+    return r;
+}
+
+ACLFFT_API aclfftResult aclfftPlan2d(aclfftHandle* plan, int batch, int nx, int ny, aclfftType type)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) {
+        GFFT_LOG("aclfftPlan2d: type=%d has no 2D execution implementation yet", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
+    aclfftResult r = aclfftCreate(plan);
+    if (r != ACLFFT_SUCCESS) return r;
+    r = aclfftMakePlan2d(*plan, batch, nx, ny, type, nullptr);
+    if (r != ACLFFT_SUCCESS) {
+        aclfftDestroy(*plan);
+        *plan = nullptr;
+    }
+    return r;
+}
+
+ACLFFT_API aclfftResult aclfftPlan3d(aclfftHandle* plan, int nx, int ny, int nz, aclfftType type)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    aclfftResult r = aclfftCreate(plan);
+    if (r != ACLFFT_SUCCESS) return r;
+    r = aclfftMakePlan3d(*plan, nx, ny, nz, type, nullptr);
+    if (r != ACLFFT_SUCCESS) {
+        aclfftDestroy(*plan);
+        *plan = nullptr;
+    }
+    return r;
+}
+
+ACLFFT_API aclfftResult aclfftSetStream(aclfftHandle plan, cudaStream_t stream)
+{
+    ACLFFT_CHECK_NULL(plan);
+    plan->stream = stream;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftDestroy(aclfftHandle plan)
+{
+    ACLFFT_CHECK_NULL(plan);
+    delete plan;
+    return ACLFFT_SUCCESS;
+}
+
+}  // extern "C"

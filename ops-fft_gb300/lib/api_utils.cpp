@@ -1,0 +1,173 @@
+// api_utils.cpp - error strings, the reference's NOT_IMPLEMENTED stubs and
+// the GB300 extension getters/setters.
+//
+// aclfftGetErrorString follows lib/fft_utils_api.cpp:19-56 of the reference
+// (same strings, "Unknown error" otherwise); the work-area, stride and
+// version entries are stubs there too (lib/fft_utils_api.cpp:66-109).
+#include <algorithm>
+#include <cstring>
+
+#include "handle.h"
+
+namespace gfft {
+
+bool log_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("OPS_FFT_LOG");
+        return !(v && (std::strcmp(v, "0") == 0 || std::strcmp(v, "off") == 0));
+    }();
+    return on;
+}
+
+}  // namespace gfft
+
+extern "C" {
+
+ACLFFT_API const char* aclfftGetErrorString(aclfftResult result)
+{
+    switch (result) {
+    case ACLFFT_SUCCESS: return "Success";
+    case ACLFFT_INVALID_PLAN: return "Invalid plan handle";
+    case ACLFFT_ALLOC_FAILED: return "Memory allocation failed";
+    case ACLFFT_INVALID_TYPE: return "Invalid data type";
+    case ACLFFT_INVALID_VALUE: return "Invalid parameter value";
+    case ACLFFT_INTERNAL_ERROR: return "Internal error";
+    case ACLFFT_EXEC_FAILED: return "Execution failed";
+    case ACLFFT_SETUP_FAILED: return "Setup failed";
+    case ACLFFT_INVALID_SIZE: return "Invalid size parameter";
+    case ACLFFT_UNALIGNED_DATA: return "Data not aligned";
+    case ACLFFT_INCOMPLETE_PARAMETER_LIST: return "Incomplete parameter list";
+    case ACLFFT_INVALID_DEVICE: return "Invalid device";
+    case ACLFFT_PARSE_ERROR: return "Parse error";
+    case ACLFFT_NO_WORKSPACE: return "No workspace available";
+    case ACLFFT_NOT_IMPLEMENTED: return "Feature not implemented";
+    case ACLFFT_NOT_SUPPORTED: return "Feature not supported";
+    default: return "Unknown error";
+    }
+}
+
+ACLFFT_API aclfftResult aclfftGetSize1d(aclfftHandle plan, int nx, aclfftType type, int batch, size_t* workSize)
+{
+    (void)plan; (void)nx; (void)type; (void)batch; (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclfftType type, size_t* workSize)
+{
+    (void)plan; (void)nx; (void)ny; (void)type; (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
+                                        size_t* workSize)
+{
+    (void)plan; (void)nx; (void)ny; (void)nz; (void)type; (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetSize(aclfftHandle plan, size_t* workSize)
+{
+    (void)plan; (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftSetAutoAllocation(aclfftHandle plan, int autoAllocate)
+{
+    (void)plan; (void)autoAllocate;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftSetWorkArea(aclfftHandle plan, void* workArea)
+{
+    (void)plan; (void)workArea;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftSetStride(aclfftHandle plan, int32_t stride)
+{
+    (void)plan; (void)stride;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetVersion(int* version)
+{
+    (void)version;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetProperty(aclfftLibraryPropertyType type, int* value)
+{
+    (void)type; (void)value;
+    return ACLFFT_NOT_IMPLEMENTED;
+}
+
+// ------------------------------------------------------------- extensions
+ACLFFT_API aclfftResult aclfftSetNormMode(aclfftHandle plan, int normMode)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_PARAM(normMode >= ACLFFT_NORM_NONE && normMode <= ACLFFT_NORM_FORWARD, ACLFFT_INVALID_VALUE);
+    plan->normMode = normMode;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftGetNormMode(aclfftHandle plan, int* normMode)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(normMode);
+    *normMode = plan->normMode;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(info);
+    std::memset(info, 0, sizeof(*info));
+    const gfft::StepList& sl = plan->impl->lists[0];
+    info->supported = sl.supported ? 1 : 0;
+    info->nsteps = (int)sl.steps.size();
+    for (const gfft::Step& s : sl.steps) {
+        const gfft::InnerPlan* ip = nullptr;
+        int tf = 0;
+        if (s.kind == gfft::Step::ROW) {
+            ip = &s.row.ip;
+            tf = s.row.tfpc;
+        } else if (s.kind == gfft::Step::COL) {
+            ip = &s.col.ip;
+            tf = s.col.tfpc;
+        }
+        if (!ip) continue;
+        info->nradix = ip->npass;
+        for (int p = 0; p < ip->npass && p < 12; ++p) info->radix[p] = ip->pass[p].radix;
+        info->onchip_length = ip->L;
+        info->threads_per_transform = ip->nthr;
+        info->transforms_per_cta = tf;
+        break;
+    }
+    info->twiddle_entries = plan->impl->tb.count;
+    info->workspace_bytes = (size_t)(plan->impl->ws_bytes + plan->impl->ws2_bytes);
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host, long long maxEntries,
+                                          long long* entries)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(entries);
+    gfft::PlanImpl* impl = plan->impl;
+    *entries = impl->tb.count;
+    if (!host || maxEntries <= 0) return ACLFFT_SUCCESS;
+    if (!impl->device_ready && gfft::plan_device_setup(impl) != ACLFFT_SUCCESS) return ACLFFT_EXEC_FAILED;
+    if (!impl->device_ready) return ACLFFT_EXEC_FAILED;
+    const long long n = std::min<long long>(maxEntries, impl->tb.count);
+    if (n > 0 && cudaMemcpy(host, impl->tw, (size_t)n * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    return ACLFFT_SUCCESS;
+}
+
+}  // extern "C"

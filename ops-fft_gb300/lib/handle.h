@@ -1,0 +1,87 @@
+// handle.h - the plan object behind aclfftHandle.
+//
+// The reference keeps only the transform description in the handle
+// (lib/fft_handle_impl.h:23-59).  Those fields are kept with the same names
+// and defaults; the GB300 plan additionally owns its device state: the FP32
+// twiddle blob generated on the GPU, the kernel step lists for each call
+// variant, the workspace and (lazily) host-staging buffers.
+#pragma once
+#include <cuda_runtime_api.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+
+#include "../../include/aclfft_ext.h"
+#include "../../include/cann_ops_fft.h"
+#include "planner.h"
+
+namespace gfft {
+
+struct PlanImpl {
+    Problem prob{};
+    // step lists: [0] primary out-of-place, [1] primary in-place,
+    //             [2] adjoint out-of-place, [3] adjoint in-place
+    StepList lists[4];
+    TwiddleBuilder tb;
+    int64_t ws_bytes = 0, ws2_bytes = 0;
+    // device state (created at plan time when a device is present)
+    bool device_ready = false;
+    int device = -1;
+    void* tw = nullptr;
+    void* ws = nullptr;
+    void* ws2 = nullptr;
+    // host staging (allocated on the first exec with host pointers)
+    void* stage_a = nullptr;
+    void* stage_b = nullptr;
+    size_t stage_bytes = 0;
+};
+
+void plan_impl_free(PlanImpl* p);
+aclfftResult plan_device_setup(PlanImpl* p);
+
+void set_last_error(const std::string& s);
+bool log_enabled();
+
+}  // namespace gfft
+
+struct aclfftHandle_t {
+    int32_t rank;
+    int32_t lengths[3];
+    int32_t stride[3];
+    int32_t batch;
+    aclfftType type;
+    int32_t normMode;
+    cudaStream_t stream;
+    bool is_initialized;
+    gfft::PlanImpl* impl;
+
+    aclfftHandle_t()
+        : rank(0), lengths{0, 0, 0}, stride{0, 0, 0}, batch(1), type(ACLFFT_C2C), normMode(0), stream(nullptr),
+          is_initialized(false), impl(nullptr)
+    {
+    }
+    ~aclfftHandle_t()
+    {
+        if (impl) {
+            gfft::plan_impl_free(impl);
+            delete impl;
+        }
+    }
+};
+
+#define GFFT_LOG(...)                                   \
+    do {                                                \
+        if (gfft::log_enabled()) {                      \
+            std::fprintf(stderr, "[ops-fft] ");         \
+            std::fprintf(stderr, __VA_ARGS__);          \
+            std::fprintf(stderr, "\n");                 \
+        }                                               \
+    } while (0)
+
+#define ACLFFT_CHECK_PARAM(cond, code) \
+    do {                               \
+        if (!(cond)) return (code);    \
+    } while (0)
+#define ACLFFT_CHECK_NULL(p) ACLFFT_CHECK_PARAM((p) != nullptr, ACLFFT_INVALID_VALUE)

@@ -1,0 +1,225 @@
+// plan_check.cpp - host-side verification of a plan's launches.
+//
+// Replays the address arithmetic of every kernel launch the plan can make
+// (all four call variants) and checks it against the sizes of the buffers
+// the launch will receive: user input/output for the call shape, the
+// plan's workspaces and its twiddle blob, plus launch-shape limits (threads,
+// dynamic shared memory, grid size).  Used by the CPU test-suite so index
+// errors are caught without running a kernel.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "handle.h"
+
+namespace {
+
+using namespace gfft;
+
+struct Bufs {
+    int64_t bytes[4];  // in, out, ws, ws2
+};
+
+int spad_host(int i) { return i + (i >> 4); }
+
+bool fail(std::string& why, const std::string& s)
+{
+    why = s;
+    return false;
+}
+
+bool check_inner(const InnerPlan& ip, int64_t tw_count, std::string& why)
+{
+    if (ip.L < 1 || ip.npass < 1 || ip.npass > kMaxPass) return fail(why, "bad inner plan");
+    int64_t ns = 1;
+    for (int p = 0; p < ip.npass; ++p) {
+        const PassDesc& d = ip.pass[p];
+        if (d.radix < 1 || d.radix > 47) return fail(why, "bad radix");
+        if (d.radix > 16 && ip.rmax != 47) return fail(why, "radix beyond kernel instantiation");
+        if (d.ns != ns) return fail(why, "ns mismatch");
+        if (ns > 1) {
+            if (d.tw_off < 0 || d.tw_off + ns * d.radix > tw_count) return fail(why, "pass twiddle out of table");
+            if (d.radix % 2 == 0 && (d.tw_off % 2) != 0) return fail(why, "pass twiddle misaligned for float4");
+            if (ns >= 65536 || ip.L >= 65536) return fail(why, "fast division range exceeded");
+            // verify the magic division for every j that occurs
+            const int nbf = ip.L / d.radix;
+            for (int j = 0; j < nbf; ++j) {
+                const unsigned q = (unsigned)(((uint64_t)(unsigned)j * d.ns_magic) >> 32);
+                if ((int64_t)q != j / ns) return fail(why, "magic division wrong");
+            }
+        }
+        ns *= d.radix;
+    }
+    if (ns != ip.L) return fail(why, "radix product != L");
+    if (ip.nthr < 1) return fail(why, "no threads");
+    return true;
+}
+
+// Highest shared buffer (1 = A, 2 = B) that run_passes touches.
+int buffers_used(int npass, int start, bool last_global)
+{
+    int cur = start, used = start;
+    for (int p = 0; p < npass; ++p) {
+        const int dst = (last_global && p == npass - 1) ? 0 : (cur == 1 ? 2 : 1);
+        used = std::max(used, dst);
+        cur = dst;
+    }
+    return used;
+}
+
+bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
+{
+    const RowArgs& a = s.row;
+    if (!check_inner(a.ip, tw_count, why)) return false;
+    const int L = a.ip.L;
+    const int maxthr = a.ip.rmax == 16 ? 512 : 256;
+    if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1) return fail(why, "row threads");
+    if ((int64_t)a.tfpc * a.nbuf * a.lpad * 8 > kMaxSmemBytes) return fail(why, "row smem");
+    const bool even = a.io_mode == IO_R2C_EVEN || a.io_mode == IO_C2R_EVEN;
+    if (spad_host(even ? L : L - 1) >= a.lpad) return fail(why, "row lpad too small");
+    {
+        int start = 0;
+        bool last_global = true;
+        if (a.io_mode == IO_C2C && a.staged) {
+            start = 1;
+            last_global = false;
+        } else if (a.io_mode == IO_R2C_EVEN) {
+            last_global = false;
+            start = a.staged ? 1 : 0;
+        } else if (a.io_mode == IO_C2R_EVEN) {
+            start = 1;
+        }
+        if (buffers_used(a.ip.npass, start, last_global) > a.nbuf) return fail(why, "row needs more shared buffers");
+    }
+    if ((a.ntf + a.tfpc - 1) / a.tfpc > 0x7fffffff) return fail(why, "row grid");
+    if (a.staged && (int64_t)a.tfpc * (L + 1) >= (1 << 22)) return fail(why, "staged copy index range");
+    int64_t in_last = 0, out_last = 0, in_es = 8, out_es = 8;
+    const int N = a.nreal;
+    switch (a.io_mode) {
+    case IO_C2C: in_last = L - 1; out_last = L - 1; break;
+    case IO_R2C_EVEN: in_last = L - 1; out_last = L; break;
+    case IO_C2R_EVEN: in_last = L; out_last = L - 1; break;
+    case IO_R2C_ODD: in_es = 4; in_last = N - 1; out_last = N / 2; break;
+    case IO_C2R_ODD: in_last = N / 2; out_es = 4; out_last = N - 1; break;
+    default: return fail(why, "io mode");
+    }
+    if (((a.ntf - 1) * a.in_dist + in_last + 1) * in_es > b.bytes[s.src]) return fail(why, "row input out of bounds");
+    if (((a.ntf - 1) * a.out_dist + out_last + 1) * out_es > b.bytes[s.dst]) return fail(why, "row output out of bounds");
+    if (even && (s.post_off < 0 || s.post_off + L / 2 + 1 > tw_count)) return fail(why, "post twiddle out of table");
+    return true;
+}
+
+int64_t max_part(int64_t cpi, int64_t split, int64_t hi, int64_t lo)
+{
+    const int64_t jmax = cpi - 1;
+    return (jmax / split) * hi + std::min(split - 1, jmax) * lo;
+}
+
+bool check_col(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
+{
+    const ColArgs& a = s.col;
+    if (!check_inner(a.ip, tw_count, why)) return false;
+    const int L = a.ip.L;
+    const int maxthr = a.ip.rmax == 16 ? 512 : 256;
+    if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1 || a.tfp < a.tfpc) return fail(why, "col threads");
+    if ((int64_t)a.nbuf * L * a.tfp * 8 > kMaxSmemBytes) return fail(why, "col smem");
+    if (buffers_used(a.ip.npass, 0, !a.staged_out) > a.nbuf) return fail(why, "col needs more shared buffers");
+    if ((a.ncols + a.tfpc - 1) / a.tfpc > 0x7fffffff) return fail(why, "col grid");
+    if (a.cpi < 1 || a.ncols % a.cpi != 0) return fail(why, "col cpi");
+    const int64_t items = a.ncols / a.cpi;
+    const int64_t in_max = (items - 1) * a.in_dist + max_part(a.cpi, a.in_split, a.in_hi, a.in_lo) +
+                           (int64_t)(L - 1) * a.in_stride;
+    if ((in_max + 1) * 8 > b.bytes[s.src]) return fail(why, "col input out of bounds");
+    int64_t out_max;
+    if (a.staged_out) {
+        out_max = a.ncols * L - 1;
+    } else {
+        out_max = (items - 1) * a.out_dist + max_part(a.cpi, a.out_split, a.out_hi, a.out_lo) +
+                  (int64_t)(L - 1) * a.out_stride;
+    }
+    if ((out_max + 1) * 8 > b.bytes[s.dst]) return fail(why, "col output out of bounds");
+    if (a.ons > 1) {
+        const int64_t M = a.ons * L;
+        if (M >= (int64_t(1) << 32)) return fail(why, "outer twiddle index overflow");
+        const int64_t S = int64_t(1) << a.otw_shift;
+        if (s.lo_off < 0 || s.lo_off + S > tw_count) return fail(why, "outer lo table");
+        if (s.hi_off < 0 || s.hi_off + (M + S - 1) / S > tw_count) return fail(why, "outer hi table");
+        if (a.tw_div < 1) return fail(why, "tw_div");
+    }
+    return true;
+}
+
+bool check_pack(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
+{
+    const PackArgs& a = s.pack;
+    const int64_t L = a.L;
+    const int64_t in_last = a.c2r ? L : L - 1, out_last = a.c2r ? L - 1 : L;
+    if (((a.ntf - 1) * a.in_dist + in_last + 1) * 8 > b.bytes[s.src]) return fail(why, "pack input out of bounds");
+    if (((a.ntf - 1) * a.out_dist + out_last + 1) * 8 > b.bytes[s.dst]) return fail(why, "pack output out of bounds");
+    if (s.post_off < 0 || s.post_off + L / 2 + 1 > tw_count) return fail(why, "pack twiddles");
+    return true;
+}
+
+}  // namespace
+
+extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int msglen)
+{
+    auto report = [&](const std::string& s) {
+        if (msg && msglen > 0) {
+            std::snprintf(msg, (size_t)msglen, "%s", s.c_str());
+        }
+    };
+    if (!plan || !plan->impl) {
+        report("no plan");
+        return -1;
+    }
+    PlanImpl* impl = plan->impl;
+    const Problem& p = impl->prob;
+    int64_t cbytes, rbytes, hbytes;
+    if (p.rank == 2) {
+        cbytes = p.batch * p.n0 * p.n1 * 8;
+    } else {
+        cbytes = p.batch * p.n0 * std::max<int64_t>(p.stride, 1) * 8;
+    }
+    rbytes = p.batch * p.n0 * 4;
+    hbytes = p.batch * (p.n0 / 2 + 1) * 8;
+    for (int v = 0; v < 4; ++v) {
+        const StepList& sl = impl->lists[v];
+        if (!sl.supported) continue;
+        Bufs b{};
+        int64_t in_b = cbytes, out_b = cbytes;
+        const bool adj = v >= 2;
+        if (p.kind == Kind::R2C) {
+            in_b = adj ? hbytes : rbytes;
+            out_b = adj ? rbytes : hbytes;
+        } else if (p.kind == Kind::C2R) {
+            in_b = adj ? rbytes : hbytes;
+            out_b = adj ? hbytes : rbytes;
+        }
+        const bool inplace = (v & 1) != 0;
+        b.bytes[0] = inplace ? 0 : in_b;
+        b.bytes[1] = inplace ? std::max(in_b, out_b) : out_b;
+        b.bytes[2] = impl->ws_bytes;
+        b.bytes[3] = impl->ws2_bytes;
+        for (size_t i = 0; i < sl.steps.size(); ++i) {
+            const Step& s = sl.steps[i];
+            std::string why;
+            bool ok = true;
+            if (s.src < 0 || s.src > 3 || s.dst < 0 || s.dst > 3) ok = fail(why, "buffer id");
+            else if (s.kind == Step::ROW) ok = check_row(s, b, impl->tb.count, why);
+            else if (s.kind == Step::COL) ok = check_col(s, b, impl->tb.count, why);
+            else if (s.kind == Step::PACK) ok = check_pack(s, b, impl->tb.count, why);
+            else if (s.kind == Step::COPY)
+                ok = (s.copy_bytes <= b.bytes[s.src] && s.copy_bytes <= b.bytes[s.dst]) || fail(why, "copy size");
+            if (!ok) {
+                char buf[160];
+                std::snprintf(buf, sizeof(buf), "variant %d step %zu: ", v, i);
+                report(buf + why);
+                return 1 + v;
+            }
+        }
+    }
+    report("ok");
+    return 0;
+}

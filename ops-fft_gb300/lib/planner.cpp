@@ -1,0 +1,507 @@
+// planner.cpp - see planner.h.
+#include "planner.h"
+
+#include <algorithm>
+#include <cmath>
+#include <functional>
+
+namespace gfft {
+
+namespace {
+
+constexpr int kBigPrimes[] = {17, 19, 23, 29, 31, 37, 41, 43, 47};
+
+int spad_host(int i) { return i + (i >> 4); }
+
+int max_threads_for(int rmax) { return rmax <= 16 ? 512 : 256; }
+
+int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+std::vector<int64_t> prime_factors(int64_t n)
+{
+    std::vector<int64_t> f;
+    if (n <= 1) return f;
+    for (int64_t p = 2; p * p <= n; ++p) {
+        while (n % p == 0) {
+            f.push_back(p);
+            n /= p;
+        }
+    }
+    if (n > 1) f.push_back(n);
+    return f;
+}
+
+bool all_primes_at_most(int64_t n, int64_t pmax)
+{
+    for (int64_t p : prime_factors(n))
+        if (p > pmax) return false;
+    return true;
+}
+
+bool length_supported(int64_t n) { return n >= 1 && all_primes_at_most(n, 47); }
+
+std::vector<int> choose_radices(int L)
+{
+    if (L == 1) return {1};
+    if (!all_primes_at_most(L, 47)) return {};
+    std::vector<int> allowed;
+    for (int r = 16; r >= 2; --r) allowed.push_back(r);
+    for (int p : kBigPrimes)
+        if (L % p == 0) allowed.insert(allowed.begin(), p);
+    std::sort(allowed.begin(), allowed.end(), std::greater<int>());
+
+    std::vector<int> best, cur;
+    int best_pass = 1 << 30, best_min = 0, best_pow2 = -1;
+    std::function<void(int, int)> dfs = [&](int rem, int maxr) {
+        if ((int)cur.size() > best_pass || (int)cur.size() >= kMaxPass) return;
+        if (rem == 1) {
+            const int np = (int)cur.size();
+            const int mn = *std::min_element(cur.begin(), cur.end());
+            int pow2 = 0;
+            for (int r : cur) pow2 += ((r & (r - 1)) == 0);
+            if (np < best_pass || (np == best_pass && (mn > best_min || (mn == best_min && pow2 > best_pow2)))) {
+                best = cur;
+                best_pass = np;
+                best_min = mn;
+                best_pow2 = pow2;
+            }
+            return;
+        }
+        for (int r : allowed) {
+            if (r > maxr || rem % r) continue;
+            cur.push_back(r);
+            dfs(rem / r, r);
+            cur.pop_back();
+        }
+    };
+    dfs(L, 1 << 30);
+    return best;
+}
+
+int64_t TwiddleBuilder::add_pass_table(int64_t ns, int R)
+{
+    for (const TwSeg& t : segs)
+        if (t.kind == 0 && t.M == ns * R && t.R_or_mult == R) return t.offset;
+    const int64_t off = count;
+    TwSeg s{};
+    s.offset = off;
+    s.count = ns * R;
+    s.M = ns * R;
+    s.R_or_mult = R;
+    s.kind = 0;
+    segs.push_back(s);
+    count += ns * R;
+    count += count & 1;
+    return off;
+}
+
+int64_t TwiddleBuilder::add_linear(int64_t n, int64_t M, int64_t mult)
+{
+    for (const TwSeg& t : segs)
+        if (t.kind == 1 && t.M == M && t.R_or_mult == mult && t.count >= n) return t.offset;
+    const int64_t off = count;
+    TwSeg s{};
+    s.offset = off;
+    s.count = n;
+    s.M = M;
+    s.R_or_mult = mult;
+    s.kind = 1;
+    segs.push_back(s);
+    count += n;
+    count += count & 1;
+    return off;
+}
+
+bool build_inner(int L, const std::vector<int>& radices, int nthr, TwiddleBuilder& tb, InnerPlan& ip)
+{
+    if (radices.empty() || (int)radices.size() > kMaxPass) return false;
+    ip = InnerPlan{};
+    ip.L = L;
+    ip.npass = (int)radices.size();
+    ip.nthr = nthr;
+    ip.rmax = 16;
+    int64_t ns = 1;
+    for (int p = 0; p < ip.npass; ++p) {
+        const int R = radices[p];
+        if (R > 16) ip.rmax = 47;
+        PassDesc& d = ip.pass[p];
+        d.radix = R;
+        d.ns = (int32_t)ns;
+        d.ns_magic = ns > 1 ? (uint32_t)(((1ull << 32) + (uint64_t)ns - 1) / (uint64_t)ns) : 0u;
+        d.tw_off = ns > 1 ? (int32_t)tb.add_pass_table(ns, R) : -1;
+        ns *= R;
+    }
+    return ns == L;
+}
+
+namespace {
+
+int pick_nthr(int L, const std::vector<int>& radices, int maxthr)
+{
+    int nbf_max = 1;
+    for (int r : radices) nbf_max = std::max(nbf_max, L / r);
+    if (nbf_max <= maxthr) return nbf_max;
+    return (int)ceil_div(nbf_max, ceil_div(nbf_max, maxthr));
+}
+
+// Shared-memory buffers a row transform needs (see row_body in stockham.cuh).
+int row_nbuf(int npass, int start, bool last_global)
+{
+    const int writes = npass - (last_global ? 1 : 0);
+    if (start == 1) return writes >= 1 ? 2 : 1;
+    return writes >= 2 ? 2 : 1;
+}
+
+}  // namespace
+
+// Largest lengths accepted by the generic kernels (checked exactly below).
+int row_max_length() { return 13312; }
+int col_max_length() { return 2048; }
+
+namespace {
+
+// One on-chip transform per contiguous batch item.
+bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io_mode, int nreal, int weight,
+                   TwiddleBuilder& tb, Step& st)
+{
+    std::vector<int> rad = choose_radices(L);
+    if (rad.empty()) return false;
+    const int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
+    const int maxthr = max_threads_for(rmax);
+    const int nthr = pick_nthr(L, rad, maxthr);
+    const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
+    const bool staged = nthr < 32 && (io_mode == IO_C2C || even_mode);
+    const int start = (io_mode == IO_C2R_EVEN || staged) ? 1 : 0;
+    const bool last_global = !(io_mode == IO_R2C_EVEN || staged);
+    const int nbuf = row_nbuf((int)rad.size(), start, last_global);
+    int lpad = spad_host(L) + 2;
+    lpad += lpad & 1;
+    const int64_t per_tf = (int64_t)nbuf * lpad * 8;
+    if (per_tf > kMaxSmemBytes) return false;
+    int tf = std::max(1, 256 / nthr);
+    tf = std::min(tf, maxthr / nthr);
+    tf = (int)std::min<int64_t>(tf, std::max<int64_t>(1, (96 * 1024) / per_tf));
+    tf = (int)std::min<int64_t>(tf, ntf);
+    tf = std::max(tf, 1);
+
+    st = Step{};
+    st.kind = Step::ROW;
+    RowArgs& a = st.row;
+    if (!build_inner(L, rad, nthr, tb, a.ip)) return false;
+    a.ntf = ntf;
+    a.in_dist = in_dist;
+    a.out_dist = out_dist;
+    a.tfpc = tf;
+    a.lpad = lpad;
+    a.nbuf = nbuf;
+    a.io_mode = io_mode;
+    a.weight = weight;
+    a.nreal = nreal;
+    a.staged = staged ? 1 : 0;
+    a.scale = 1.f;
+    a.conj_out = io_mode == IO_C2R_EVEN ? 1 : 0;
+    st.tw_off = 0;
+    if (even_mode) st.post_off = tb.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
+    return true;
+}
+
+// One column pass over an axis of length n (stride S between samples, S
+// independent columns per item, `items` items `D` apart).  The pass runs the
+// q-th factor Lq of the axis decomposition after a product Ns of earlier
+// factors (outer Stockham pass); Ns == 1 and Lq == n is a plain strided
+// transform.
+bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64_t Ns, TwiddleBuilder& tb, Step& st)
+{
+    std::vector<int> rad = choose_radices(Lq);
+    if (rad.empty()) return false;
+    const int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
+    const int maxthr = max_threads_for(rmax);
+    const bool staged_out = (S == 1 && Ns == 1 && Lq != n);
+    const int writes = (int)rad.size() - (staged_out ? 0 : 1);
+    const int nbuf = writes >= 2 ? 2 : 1;
+    const int64_t cpi = (n / Lq) * S;
+    // widest column group that fits
+    int tf = 16;
+    int nthr = 1;
+    for (; tf >= 1; tf >>= 1) {
+        const int tfp = tf + 1;
+        if ((int64_t)nbuf * Lq * tfp * 8 > kMaxSmemBytes) continue;
+        nthr = pick_nthr(Lq, rad, std::max(1, maxthr / tf));
+        if (nthr * tf > maxthr) continue;
+        if ((int64_t)nbuf * Lq * tfp * 8 > 110 * 1024 && tf > 4) continue;
+        break;
+    }
+    if (tf < 1) return false;
+    st = Step{};
+    st.kind = Step::COL;
+    ColArgs& a = st.col;
+    if (!build_inner(Lq, rad, nthr, tb, a.ip)) return false;
+    a.ncols = items * cpi;
+    a.cpi = cpi;
+    a.in_dist = D;
+    a.in_split = cpi;
+    a.in_hi = 0;
+    a.in_lo = 1;
+    a.in_stride = (n / Lq) * S;
+    a.out_dist = D;
+    a.out_split = Ns * S;
+    a.out_hi = Ns * Lq * S;
+    a.out_lo = 1;
+    a.out_stride = Ns * S;
+    a.ons = Ns;
+    a.tw_div = S;
+    a.tfpc = tf;
+    a.tfp = tf + 1;
+    a.nbuf = nbuf;
+    a.staged_out = staged_out ? 1 : 0;
+    a.scale = 1.f;
+    st.tw_off = 0;
+    if (Ns > 1) {
+        const int64_t M = Ns * Lq;
+        int shift = 0;
+        while ((int64_t(1) << (2 * shift)) < M) ++shift;  // 2^shift >= sqrt(M)
+        a.otw_shift = shift;
+        st.lo_off = tb.add_linear(int64_t(1) << shift, M, 1);
+        st.hi_off = tb.add_linear(ceil_div(M, int64_t(1) << shift), M, int64_t(1) << shift);
+    }
+    return true;
+}
+
+// Strided-axis transform as a list of column passes with buffer routing.
+bool make_axis_steps(int64_t n, int64_t S, int64_t items, int64_t D, int src, int dst, int spare, int cap,
+                     TwiddleBuilder& tb, std::vector<Step>& out, bool& needs_spare)
+{
+    std::vector<int> fac = split_axis(n, cap);
+    if (fac.empty()) return false;
+    const int Q = (int)fac.size();
+    // routing: pass q reads b[q] and writes b[q+1].  Only the last pass may
+    // run in place (its read set equals its write set); every other pass
+    // must write a buffer different from the one it reads, and `src` may be
+    // reused as scratch only after the first pass consumed it.
+    std::vector<int> b(Q + 1);
+    b[0] = src;
+    b[Q] = dst;
+    if (Q >= 2) {
+        b[Q - 1] = dst;
+        for (int q = Q - 2; q >= 1; --q) b[q] = (b[q + 1] == dst) ? spare : dst;
+        if (b[1] == src) {
+            if (Q != 2) return false;
+            b[1] = spare;
+        }
+    }
+    needs_spare = false;
+    int64_t Ns = 1;
+    for (int q = 0; q < Q; ++q) {
+        Step st;
+        if (!make_col_step(n, S, items, D, fac[q], Ns, tb, st)) return false;
+        st.src = b[q];
+        st.dst = b[q + 1];
+        if (st.src == spare || st.dst == spare) needs_spare = true;
+        out.push_back(st);
+        Ns *= fac[q];
+    }
+    return true;
+}
+
+bool row_feasible(int L, int io_mode)
+{
+    std::vector<int> rad = choose_radices(L);
+    if (rad.empty()) return false;
+    const int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
+    const int nthr = pick_nthr(L, rad, max_threads_for(rmax));
+    const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
+    const bool staged = nthr < 32 && (io_mode == IO_C2C || even_mode);
+    const int start = (io_mode == IO_C2R_EVEN || staged) ? 1 : 0;
+    const bool last_global = !(io_mode == IO_R2C_EVEN || staged);
+    const int nbuf = row_nbuf((int)rad.size(), start, last_global);
+    const int64_t lpad = spad_host(L) + 3;
+    return nbuf * lpad * 8 <= kMaxSmemBytes;
+}
+
+}  // namespace
+
+std::vector<int> split_axis(int64_t n, int cap)
+{
+    if (!length_supported(n)) return {};
+    if (n <= cap) return {(int)n};
+    // smallest number of factors; balanced (closest to n^(1/Q))
+    std::vector<int64_t> divs;
+    for (int64_t d = 2; d <= cap && d < n; ++d)
+        if (n % d == 0) divs.push_back(d);
+    for (int Q = 2; Q <= 4; ++Q) {
+        const double target = std::pow((double)n, 1.0 / Q);
+        std::vector<int> best;
+        double best_score = 1e300;
+        std::vector<int> cur;
+        std::function<void(int64_t, int)> dfs = [&](int64_t rem, int left) {
+            if (left == 1) {
+                if (rem > cap || rem < 2) return;
+                cur.push_back((int)rem);
+                double score = 0;
+                for (int f : cur) score += std::fabs(std::log((double)f / target));
+                if (score < best_score) {
+                    best_score = score;
+                    best = cur;
+                }
+                cur.pop_back();
+                return;
+            }
+            for (int64_t d : divs) {
+                if (rem % d || rem / d < 2) continue;
+                cur.push_back((int)d);
+                dfs(rem / d, left - 1);
+                cur.pop_back();
+            }
+        };
+        dfs(n, Q);
+        if (!best.empty()) {
+            // largest factor first: the first pass writes contiguous blocks
+            std::sort(best.begin(), best.end(), std::greater<int>());
+            return best;
+        }
+    }
+    return {};
+}
+
+bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
+                 int64_t& ws2_bytes)
+{
+    out = StepList{};
+    ws_bytes = 0;
+    ws2_bytes = 0;
+    auto unsupported = [&](const char* why) {
+        out.supported = false;
+        out.why = why;
+        return true;
+    };
+    const int cap = col_max_length();
+    const int IN = inplace ? BUF_OUT : BUF_IN;
+    auto need_ws = [&](int64_t bytes) { ws_bytes = std::max(ws_bytes, bytes); };
+    auto need_ws2 = [&](int64_t bytes) { ws2_bytes = std::max(ws2_bytes, bytes); };
+
+    if (p.rank == 2) {
+        if (p.kind != Kind::C2C) return unsupported("2D supports C2C only");
+        const int64_t nx = p.n0, ny = p.n1;
+        if (!length_supported(nx) || !length_supported(ny)) return unsupported("2D length has a prime factor > 47");
+        const int64_t bytes = p.batch * nx * ny * 8;
+        // rows (contiguous, length ny) then columns (length nx, stride ny)
+        bool spare = false;
+        if (ny <= row_max_length() && row_feasible((int)ny, IO_C2C)) {
+            Step st;
+            if (!make_row_step((int)ny, p.batch * nx, ny, ny, IO_C2C, 0, WEIGHT_NONE, tb, st)) return false;
+            st.src = IN;
+            st.dst = BUF_OUT;
+            out.steps.push_back(st);
+        } else if (!make_axis_steps(ny, 1, p.batch * nx, ny, IN, BUF_OUT, BUF_WS, cap, tb, out.steps, spare)) {
+            return unsupported("2D row length not decomposable");
+        }
+        if (spare) need_ws(bytes);
+        if (!make_axis_steps(nx, ny, p.batch, nx * ny, BUF_OUT, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
+            return unsupported("2D column length not decomposable");
+        if (spare) need_ws(bytes);
+        return true;
+    }
+
+    const int64_t N = p.n0;
+    if (!length_supported(N)) return unsupported("length has a prime factor > 47");
+
+    if (p.kind == Kind::C2C) {
+        bool spare = false;
+        if (p.stride > 1) {
+            // VERTICAL: transforms down the columns of [N][stride]
+            if (!make_axis_steps(N, p.stride, 1, N * p.stride, IN, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
+                return unsupported("vertical length not decomposable");
+            if (spare) need_ws(N * p.stride * 8);
+            return true;
+        }
+        if (N <= row_max_length() && row_feasible((int)N, IO_C2C)) {
+            Step st;
+            if (!make_row_step((int)N, p.batch, N, N, IO_C2C, 0, WEIGHT_NONE, tb, st)) return false;
+            st.src = IN;
+            st.dst = BUF_OUT;
+            out.steps.push_back(st);
+            return true;
+        }
+        if (!make_axis_steps(N, 1, p.batch, N, IN, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
+            return unsupported("length not decomposable");
+        if (spare) need_ws(N * p.batch * 8);
+        return true;
+    }
+
+    if (p.stride > 1) return unsupported("VERTICAL layout is not supported for R2C/C2R");
+    const bool r2c = p.kind == Kind::R2C;
+    const int64_t nb = N / 2 + 1;
+    const int64_t in_bytes = r2c ? N * p.batch * 4 : nb * p.batch * 8;
+    // A single fused kernel reads rows of one pitch and writes rows of
+    // another, so an in-place call first copies the input to the workspace.
+    auto single = [&](int io_mode, int L, int64_t in_dist, int64_t out_dist) {
+        Step st;
+        if (!make_row_step(L, p.batch, in_dist, out_dist, io_mode, (int)N, p.weight, tb, st)) return false;
+        int src = IN;
+        if (inplace) {
+            Step cp;
+            cp.kind = Step::COPY;
+            cp.copy_bytes = in_bytes;
+            cp.src = BUF_OUT;
+            cp.dst = BUF_WS;
+            out.steps.push_back(cp);
+            need_ws(in_bytes);
+            src = BUF_WS;
+        }
+        st.src = src;
+        st.dst = BUF_OUT;
+        out.steps.push_back(st);
+        return true;
+    };
+    if (N % 2 == 0) {
+        const int64_t L = N / 2;
+        const int mode = r2c ? IO_R2C_EVEN : IO_C2R_EVEN;
+        if (L <= row_max_length() && row_feasible((int)L, mode)) {
+            if (!single(mode, (int)L, r2c ? L : nb, r2c ? nb : L)) return false;
+            return true;
+        }
+        // long real transforms: separate packing around a multi-pass C2C
+        Step pk;
+        pk.kind = Step::PACK;
+        pk.pack.L = (int)L;
+        pk.pack.ntf = p.batch;
+        pk.pack.c2r = r2c ? 0 : 1;
+        pk.pack.weight = p.weight;
+        pk.pack.scale = 1.f;
+        pk.post_off = tb.add_linear(L / 2 + 1, N, 1);
+        bool spare = false;
+        if (r2c) {
+            // input (float2 view) -> ... -> WS, then pack WS -> out
+            if (!make_axis_steps(L, 1, p.batch, L, IN, BUF_WS, BUF_WS2, cap, tb, out.steps, spare))
+                return unsupported("length not decomposable");
+            pk.pack.in_dist = L;
+            pk.pack.out_dist = nb;
+            pk.src = BUF_WS;
+            pk.dst = BUF_OUT;
+            out.steps.push_back(pk);
+        } else {
+            pk.pack.in_dist = nb;
+            pk.pack.out_dist = L;
+            pk.src = IN;
+            pk.dst = BUF_WS;
+            out.steps.push_back(pk);
+            if (!make_axis_steps(L, 1, p.batch, L, BUF_WS, BUF_OUT, BUF_WS2, cap, tb, out.steps, spare))
+                return unsupported("length not decomposable");
+            out.steps.back().col.conj_out = 1;
+        }
+        need_ws(L * p.batch * 8);
+        if (spare) need_ws2(L * p.batch * 8);
+        return true;
+    }
+    // odd N: full-length complex transform inside one CTA
+    const int mode = r2c ? IO_R2C_ODD : IO_C2R_ODD;
+    if (N <= row_max_length() && row_feasible((int)N, mode)) {
+        if (!single(mode, (int)N, r2c ? N : nb, r2c ? nb : N)) return false;
+        return true;
+    }
+    return unsupported("odd real-data length beyond one CTA");
+}
+
+}  // namespace gfft

@@ -1,0 +1,89 @@
+// planner.h - plan-time decisions for the GB300 aclfft library.
+//
+// Pure host code (no CUDA calls), so it is unit-testable without a GPU.
+// Responsibilities that the reference defers to every exec call
+// (src/fft1_d/arch35/fft/fft1_d_c2c.cpp:82-136,188-239) happen once here:
+//   * prime factorisation and the support decision (primes <= 47, the
+//     reference's RADIX_MIX set, src/common/host/fft_exec_helper.h:76);
+//   * the radix sequence of every on-chip Stockham transform;
+//   * the decomposition of long or strided axes into column passes;
+//   * the list of twiddle-table segments the GPU generator must fill;
+//   * the device workspace size.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../csrc/kernel_args.h"
+
+namespace gfft {
+
+std::vector<int64_t> prime_factors(int64_t n);  // ascending, with multiplicity
+bool all_primes_at_most(int64_t n, int64_t pmax);
+
+// Largest on-chip lengths (complex elements) the generic kernels accept.
+int row_max_length();
+int col_max_length();
+
+// Radix sequence for an on-chip transform of length L (product == L),
+// radices <= 16 when possible, primes up to 47 otherwise.  Empty on failure.
+std::vector<int> choose_radices(int L);
+
+// Split an axis of length n into on-chip factors, each <= cap.
+std::vector<int> split_axis(int64_t n, int cap);
+
+enum BufId : int { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_WS2 = 3 };
+
+struct Step {
+    enum Kind { ROW, COL, PACK, COPY } kind = ROW;
+    int64_t copy_bytes = 0;
+    RowArgs row{};
+    ColArgs col{};
+    PackArgs pack{};
+    int src = BUF_IN;
+    int dst = BUF_OUT;
+    // Offsets (float2 units) into the plan's twiddle blob for the pointers
+    // patched at exec time; -1 when unused.
+    int64_t tw_off = -1, post_off = -1, hi_off = -1, lo_off = -1;
+};
+
+// Everything needed to run one transform kind (forward / adjoint variants
+// are separate StepLists).
+struct StepList {
+    std::vector<Step> steps;
+    bool supported = true;
+    std::string why;  // reason when unsupported
+};
+
+struct TwiddleBuilder {
+    std::vector<TwSeg> segs;
+    int64_t count = 0;  // float2 entries so far (kept 2-aligned)
+    int64_t add_pass_table(int64_t ns, int R);        // rows of R, W_{ns*R}^{k*r}
+    int64_t add_linear(int64_t count, int64_t M, int64_t mult);  // W_M^{i*mult}
+};
+
+// Fill ip for length L with the given radices; register tables in tb.
+bool build_inner(int L, const std::vector<int>& radices, int nthr, TwiddleBuilder& tb, InnerPlan& ip);
+
+// High-level builder: appends the steps of one transform to `out` and its
+// twiddle segments to `tb`.  `inplace` builds the variant used when the
+// caller passes the same buffer as input and output.  ws_bytes / ws2_bytes
+// receive the device workspace the steps need.
+enum class Kind { C2C, R2C, C2R };
+
+struct Problem {
+    Kind kind = Kind::C2C;
+    int rank = 1;
+    int64_t n0 = 1, n1 = 1;  // 1D: n0 = N. 2D: n0 = nx (slow), n1 = ny (fast)
+    int64_t batch = 1;
+    int64_t stride = 1;      // VERTICAL 1D: stride between samples (= batch), batch = 1
+    int weight = WEIGHT_NONE;
+};
+
+bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
+                 int64_t& ws2_bytes);
+
+// Which transform length families are executable (reference domain).
+bool length_supported(int64_t n);
+
+}  // namespace gfft

@@ -1,0 +1,273 @@
+"""CPU tests of the C ABI: exported symbols, argument validation and error
+codes (compared with the reference's own API layer when it was built into
+oracle/_ref), error strings and plan-time decisions.  No kernel runs here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import aclfft as A
+import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared(header):
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    return sorted(set(re.findall(r"ACLFFT_API\s+[\w\s\*]*?\b(aclfft\w+)\s*\(", txt)))
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = A.lib()
+    names = _declared("cann_ops_fft.h") + _declared("aclfft_ext.h")
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_reference_header_surface_is_kept():
+    """Every function of the reference header is declared with the same name."""
+    ref = os.path.join("/root/reference", "include", "cann_ops_fft.h")
+    if not os.path.exists(ref):
+        pytest.skip("reference tree not present")
+    ref_names = sorted(set(re.findall(r"ACLFFT_API\s+[\w\s\*]*?\b(aclfft\w+)\s*\(", open(ref).read())))
+    assert set(ref_names) <= set(_declared("cann_ops_fft.h"))
+
+
+def _ref_lib():
+    path = O.ref_lib_path()
+    if path is None:
+        pytest.skip("reference API layer not built (oracle/_ref)")
+    L = ctypes.CDLL(path)
+    for name in ("aclfftPlan1d", "aclfftPlan2d", "aclfftPlan3d"):
+        getattr(L, name).argtypes = [ctypes.POINTER(ctypes.c_void_p)] + [ctypes.c_int] * 4
+    L.aclfftCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+    L.aclfftMakePlan1d.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [ctypes.c_void_p]
+    L.aclfftMakePlan2d.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 4 + [ctypes.c_void_p]
+    L.aclfftExecC2C.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    L.aclfftExecR2C.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.aclfftExecC2R.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    L.aclfftDestroy.argtypes = [ctypes.c_void_p]
+    L.aclfftSetStream.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.aclfftGetErrorString.argtypes = [ctypes.c_int]
+    L.aclfftGetErrorString.restype = ctypes.c_char_p
+    return L
+
+
+TYPES = [A.C2C, A.R2C, A.C2R, A.Z2Z, A.D2Z, A.Z2D, 0, 0x2B, -1]
+PLAN1D_ARGS = [
+    (nx, t, b, d)
+    for nx in (0, -5, 1, 2, 7, 128, 255, 256, 300, 4096, 262144, 524288, (1 << 27), (1 << 27) + 1)
+    for t in TYPES
+    for b in (0, -1, 1, 128)
+    for d in (0, 1, 2, -1)
+]
+
+
+def _plan1d_code(L, args):
+    h = ctypes.c_void_p()
+    code = L.aclfftPlan1d(ctypes.byref(h), *args)
+    if code == 0:
+        assert h.value
+        L.aclfftDestroy(h)
+    else:
+        assert not h.value
+    return code
+
+
+def test_plan1d_error_codes_match_reference():
+    ref = _ref_lib()
+    mine = A.lib()
+    diffs = []
+    for args in PLAN1D_ARGS:
+        a, b = _plan1d_code(ref, args), _plan1d_code(mine, args)
+        if a != b:
+            diffs.append((args, a, b))
+    assert not diffs, diffs[:20]
+
+
+def test_plan2d_error_codes_match_reference_within_its_domain():
+    """The reference only accepts {32,64,128}^2; elsewhere it returns
+    NOT_SUPPORTED where this library plans the transform (documented
+    widening).  Every other code must match."""
+    ref = _ref_lib()
+    mine = A.lib()
+    for nx in (0, 32, 64, 128, 2048, 7):
+        for ny in (-1, 32, 128, 256):
+            for b in (0, 1, 8):
+                for t in TYPES:
+                    h1, h2 = ctypes.c_void_p(), ctypes.c_void_p()
+                    a = ref.aclfftPlan2d(ctypes.byref(h1), b, nx, ny, t)
+                    c = mine.aclfftPlan2d(ctypes.byref(h2), b, nx, ny, t)
+                    if a == 0:
+                        ref.aclfftDestroy(h1)
+                    if c == 0:
+                        mine.aclfftDestroy(h2)
+                    if a == A.NOT_SUPPORTED and c == 0 and t == A.C2C:
+                        continue
+                    assert a == c, (b, nx, ny, t, a, c)
+
+
+def test_exec_entry_checks_match_reference():
+    """Exec validation runs before any device work: NULL plan/buffers,
+    uninitialised plans, type mismatch and bad direction."""
+    ref = _ref_lib()
+    mine = A.lib()
+    buf = np.zeros(64, dtype=np.complex64)
+    p = buf.ctypes.data
+    for L in (ref, mine):
+        pass
+    results = {}
+    for name, L in (("ref", ref), ("mine", mine)):
+        r = []
+        r.append(L.aclfftExecC2C(None, p, p, -1))
+        h = ctypes.c_void_p()
+        L.aclfftCreate(ctypes.byref(h))
+        r.append(L.aclfftExecC2C(h, p, p, -1))  # not initialised
+        r.append(L.aclfftExecR2C(h, p, p))
+        L.aclfftDestroy(h)
+        for t in (A.C2C, A.R2C, A.C2R):
+            h = ctypes.c_void_p()
+            assert L.aclfftPlan1d(ctypes.byref(h), 8, t, 1, 0) == 0
+            r.append(L.aclfftExecC2C(h, None, p, -1))
+            r.append(L.aclfftExecC2C(h, p, None, 1))
+            r.append(L.aclfftExecR2C(h, None, p))
+            r.append(L.aclfftExecC2R(h, p, None))
+            r.append(L.aclfftExecC2C(h, p, p, 0) if t == A.C2C else L.aclfftExecC2C(h, p, p, -1))
+            r.append(L.aclfftExecC2C(h, p, p, 7) if t == A.C2C else L.aclfftExecR2C(h, p, p) if t == A.C2R else 0)
+            r.append(L.aclfftExecC2R(h, p, p) if t == A.R2C else 0)
+            L.aclfftDestroy(h)
+        results[name] = r
+    assert results["ref"] == results["mine"]
+
+
+def test_makeplan_twice_and_create_null():
+    mine = A.lib()
+    assert mine.aclfftCreate(None) == A.INVALID_VALUE
+    h = ctypes.c_void_p()
+    assert mine.aclfftCreate(ctypes.byref(h)) == 0
+    assert mine.aclfftMakePlan1d(h, 64, A.C2C, 1, 0, None) == 0
+    assert mine.aclfftMakePlan1d(h, 64, A.C2C, 1, 0, None) == A.INVALID_VALUE
+    assert mine.aclfftSetStream(h, None) == 0
+    assert mine.aclfftSetStream(None, None) == A.INVALID_VALUE
+    assert mine.aclfftDestroy(h) == 0
+    assert mine.aclfftDestroy(None) == A.INVALID_VALUE
+
+
+def test_stubs_return_not_implemented():
+    mine = A.lib()
+    h = ctypes.c_void_p()
+    sz = ctypes.c_size_t()
+    v = ctypes.c_int()
+    assert mine.aclfftGetSize1d(h, 8, A.C2C, 1, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftGetSize2d(h, 8, 8, A.C2C, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.C2C, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftGetSize(h, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftSetAutoAllocation(h, 1) == A.NOT_IMPLEMENTED
+    assert mine.aclfftSetWorkArea(h, None) == A.NOT_IMPLEMENTED
+    assert mine.aclfftSetStride(h, 2) == A.NOT_IMPLEMENTED
+    assert mine.aclfftGetVersion(ctypes.byref(v)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftGetProperty(0, ctypes.byref(v)) == A.NOT_IMPLEMENTED
+    assert mine.aclfftExecZ2Z(h, None, None, -1) == A.NOT_IMPLEMENTED
+    assert mine.aclfftExecD2Z(h, None, None) == A.NOT_IMPLEMENTED
+    assert mine.aclfftExecZ2D(h, None, None) == A.NOT_IMPLEMENTED
+    hp = ctypes.c_void_p()
+    assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, A.C2C) == A.NOT_IMPLEMENTED
+    assert not hp.value
+
+
+def test_error_strings_match_reference():
+    mine = A.lib()
+    try:
+        ref = _ref_lib()
+    except pytest.skip.Exception:
+        ref = None
+    for code in list(range(0, 20)) + [-1, 100]:
+        s = A.error_string(code)
+        assert s
+        if ref is not None:
+            assert ref.aclfftGetErrorString(code).decode() == s
+
+
+def test_norm_mode_extension():
+    p = A.Plan.plan1d(64, A.C2C)
+    for m in range(4):
+        p.set_norm(m)
+    with pytest.raises(A.AclfftError):
+        p.set_norm(4)
+    v = ctypes.c_int()
+    assert A.lib().aclfftGetNormMode(p.handle, ctypes.byref(v)) == 0 and v.value == 3
+    assert A.lib().aclfftSetNormMode(None, 0) == A.INVALID_PLAN
+
+
+@pytest.mark.parametrize(
+    "n,typ,batch,dim",
+    [(4096, A.C2C, 256, 0), (3000, A.R2C, 4096, 0), (1024, A.C2R, 4096, 0), (65536, A.C2C, 64, 0),
+     (16384, A.C2C, 64, 0), (46200, A.C2C, 1, 0), (1 << 27, A.C2C, 1, 0), (256, A.C2C, 128, 1),
+     (262144, A.C2C, 4, 1), (999, A.R2C, 1, 0), (1025, A.C2R, 4, 0), (1, A.C2C, 1, 0), (2310, A.C2C, 1, 0),
+     (5040, A.R2C, 1, 0), (25200, A.R2C, 1, 0), (1 << 25, A.R2C, 2, 0)],
+)
+def test_plan_decisions(n, typ, batch, dim):
+    """Plan-time factorisation: every on-chip transform's radices multiply to
+    its length, and the on-chip length divides the transform (bit-exact
+    integer checks of the planner, no GPU)."""
+    p = A.Plan.plan1d(n, typ, batch, dim)
+    info = p.info()
+    assert info.supported == 1
+    rad = list(info.radix)[: info.nradix]
+    assert int(np.prod(rad)) == info.onchip_length
+    half = n // 2 if (typ != A.C2C and n % 2 == 0) else n
+    assert half % info.onchip_length == 0
+    assert all(r <= 47 for r in rad)
+    assert info.threads_per_transform >= 1
+
+
+def test_unsupported_lengths_plan_but_do_not_execute():
+    """Like the reference, a length with a prime factor > 47 plans fine and is
+    rejected at exec time (NOT_IMPLEMENTED); no device work is attempted."""
+    p = A.Plan.plan1d(53 * 7, A.C2C)
+    assert p.info().supported == 0
+    buf = np.zeros(53 * 7, dtype=np.complex64)
+    assert A.lib().aclfftExecC2C(p.handle, buf.ctypes.data, buf.ctypes.data, -1) == A.NOT_IMPLEMENTED
+    pv = A.Plan.plan1d(256, A.R2C, 4, A.VERTICAL)
+    assert A.lib().aclfftExecR2C(pv.handle, buf.ctypes.data, buf.ctypes.data) == A.NOT_IMPLEMENTED
+
+
+def _sizes_for_bounds():
+    sizes = set()
+    for n in range(1, 130):
+        sizes.add(n)
+    for n in (210, 240, 250, 255, 256, 420, 512, 999, 1000, 1023, 1024, 1025, 1500, 1536, 2048, 2100, 2310, 3000,
+              4096, 5040, 6561, 8190, 8192, 12288, 13312, 13500, 15625, 16384, 16807, 25200, 26624, 32768, 46200,
+              65536, 100000, 131072, 1 << 20, 3 ** 13, 1 << 22, 1 << 25, 1 << 27, 47 * 43 * 41, 17 * 19 * 1024):
+        sizes.add(n)
+    return sorted(sizes)
+
+
+@pytest.mark.parametrize("typ", [A.C2C, A.R2C, A.C2R])
+def test_every_launch_stays_in_bounds(typ):
+    """Host replay of each planned launch's indexing against its buffers."""
+    for n in _sizes_for_bounds():
+        for b in (1, 3, 64):
+            if n * b > (1 << 28):
+                continue
+            p = A.Plan.plan1d(n, typ, b)
+            if p.info().supported:
+                p.check()
+            p.destroy()
+
+
+def test_vertical_and_2d_launches_stay_in_bounds():
+    for n in (256, 512, 4096, 65536, 262144):
+        for b in (1, 3, 128, 263168):
+            if n * b > (1 << 28):
+                continue
+            with A.Plan.plan1d(n, A.C2C, b, A.VERTICAL) as p:
+                p.check()
+    for nx, ny in ((32, 32), (64, 128), (128, 32), (2048, 2048), (7, 3000), (4096, 4096), (1, 5), (17, 19),
+                   (100000, 3), (3, 100000)):
+        with A.Plan.plan2d(2, nx, ny, A.C2C) as p:
+            if p.info().supported:
+                p.check()

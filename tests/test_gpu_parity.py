@@ -1,0 +1,404 @@
+"""GPU parity tests: every transform goes through the C ABI of libops_fft.so
+and is compared with the reference's golden vectors (its own compare rule
+and tolerances) and with the FP64 oracle at the tight FP32 bound.
+
+Tolerances (stated here, used below):
+  * plain FP32 Stockham vs FP64 oracle: rel-L2 <= 1e-5 (BASELINE target);
+  * reference golden vectors: the reference's per-case atol/rtol
+    (compare_data.py), which are looser.
+"""
+import numpy as np
+import pytest
+
+import aclfft as A
+import oracle as O
+from helpers import as_complex, cases, read_bin, regenerate
+
+pytestmark = pytest.mark.gpu
+
+REL_FP32 = 1e-5
+MAX_REGEN_ELEMS = 1 << 26
+
+torch = pytest.importorskip("torch")
+
+
+def _dev():
+    return torch.device("cuda:0")
+
+
+# ------------------------------------------------------------ host harness
+def c2c_host(n, b, x, direction, dim=A.HORIZONTAL):
+    """The reference harness flow: Plan1d -> Exec on host buffers -> Destroy."""
+    out = np.empty_like(x)
+    with A.Plan.plan1d(n, A.C2C, b, dim) as p:
+        p.exec_c2c(x, out, direction)
+    return out
+
+
+def _gold_ok(out, gold, c):
+    ok, det = O.comparison_details(out, gold, c["atol"], c["rtol"])
+    assert ok, (c["name"], det)
+
+
+def _fp64_ok(out, exact, bound=REL_FP32, what=""):
+    e = O.errors(out, exact)
+    assert e["rel_l2"] <= bound, (what, e)
+    return e
+
+
+def _fft1_case_io(c):
+    n, b = c["n"], c["batch"]
+    if "files" in c:
+        x = as_complex(read_bin("fft1_d", c["files"]["input"]).copy())
+        gold = read_bin("fft1_d", c["files"]["golden"])
+    else:
+        x = regenerate("fft1_d", c).astype(np.complex64)
+        gold = None
+    return n, b, x, gold
+
+
+@pytest.mark.parametrize("c", cases("fft1_d", include_skipped=True), ids=lambda c: c["name"])
+def test_fft1_d_reference_cases(c):
+    n, b = c["n"], c["batch"]
+    if n * b > MAX_REGEN_ELEMS:
+        pytest.skip("larger than the regenerated-case cap")
+    n, b, x, gold = _fft1_case_io(c)
+    if c.get("roundtrip"):
+        mid = c2c_host(n, b, x, A.FORWARD)
+        out = c2c_host(n, b, mid, A.BACKWARD)
+        exact = n * x.astype(np.complex128)
+        _fp64_ok(mid, O.c2c(x.reshape(b, n), -1), what="forward half")
+    elif c.get("vertical"):
+        d = A.FORWARD if c["forward"] else A.BACKWARD
+        out = c2c_host(n, b, x, d, A.VERTICAL)
+        exact = O.c2c_vertical(x.reshape(n, b), d)
+    else:
+        d = A.FORWARD if c["forward"] else A.BACKWARD
+        out = c2c_host(n, b, x, d)
+        exact = O.c2c(x.reshape(b, n), d)
+    if gold is not None:
+        _gold_ok(out, gold, c)
+    _fp64_ok(out, exact, what=c["name"])
+
+
+@pytest.mark.parametrize("c", cases("rfft1_d", include_skipped=True), ids=lambda c: c["name"])
+def test_rfft1_d_reference_cases(c):
+    n, b = c["n"], c["batch"]
+    if n * b > MAX_REGEN_ELEMS:
+        pytest.skip("larger than the regenerated-case cap")
+    if "files" in c:
+        x = read_bin("rfft1_d", c["files"]["input"]).copy()
+        gold = read_bin("rfft1_d", c["files"]["golden"])
+    else:
+        x = regenerate("rfft1_d", c)
+        gold = None
+    out = np.empty(b * (n // 2 + 1), dtype=np.complex64)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.exec_r2c(x, out)
+    if gold is not None:
+        _gold_ok(out, gold, c)
+    _fp64_ok(out, O.r2c(x.reshape(b, n)), what=c["name"])
+    # DC (and Nyquist for even n) imaginary parts are exactly zero, as in the reference
+    o = out.reshape(b, n // 2 + 1)
+    assert np.all(o[:, 0].imag == 0)
+    if n % 2 == 0:
+        assert np.all(o[:, -1].imag == 0)
+
+
+@pytest.mark.parametrize("c", cases("irfft1_d", include_skipped=True), ids=lambda c: c["name"])
+def test_irfft1_d_reference_cases(c):
+    n, b = c["n"], c["batch"]
+    X = as_complex(read_bin("irfft1_d", c["files"]["input"]).copy())
+    gold = read_bin("irfft1_d", c["files"]["golden"])
+    out = np.empty(b * n, dtype=np.float32)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.exec_c2r(X, out)
+    _gold_ok(out, gold, c)
+    _fp64_ok(out, O.c2r(X.reshape(b, n // 2 + 1), n), what=c["name"])
+
+
+@pytest.mark.parametrize("c", cases("fft2_d"), ids=lambda c: c["name"])
+def test_fft2_d_reference_cases(c):
+    nx, ny, b = c["fft_x"], c["fft_y"], c["batch"]
+    x = as_complex(read_bin("fft2_d", c["files"]["input"]).copy())
+    gold = read_bin("fft2_d", c["files"]["golden"])
+    d = A.FORWARD if c["forward"] else A.BACKWARD
+    out = np.empty_like(x)
+    with A.Plan.plan2d(b, nx, ny, A.C2C) as p:
+        p.exec_c2c(x, out, d)
+    _gold_ok(out, gold, c)
+    _fp64_ok(out, O.c2c_2d(x.reshape(b, nx, ny), d), what=c["name"])
+
+
+# --------------------------------------------------- BASELINE configurations
+def _uniform_c64(gen, shape):
+    re = torch.rand(shape, generator=gen) * 2 - 1
+    im = torch.rand(shape, generator=gen) * 2 - 1
+    return torch.complex(re, im)
+
+
+def _normal_c64(gen, shape):
+    return torch.complex(torch.randn(shape, generator=gen), torch.randn(shape, generator=gen))
+
+
+def test_config1_c2c_4096x256_device():
+    g = torch.Generator().manual_seed(12345)
+    x = _uniform_c64(g, (256, 4096))
+    xd = x.to(_dev())
+    yd = torch.empty_like(xd)
+    with A.Plan.plan1d(4096, A.C2C, 256) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2c(xd, yd, A.FORWARD)
+        torch.cuda.synchronize()
+        y = yd.cpu().numpy()
+        _fp64_ok(y, O.c2c(x.numpy(), -1), what="cfg1")
+        # same result through host buffers (staging path) and in place
+        yh = c2c_host(4096, 256, x.numpy().reshape(-1).copy(), A.FORWARD).reshape(256, 4096)
+        assert np.array_equal(yh, y)
+        p.exec_c2c(xd, xd, A.FORWARD)
+        torch.cuda.synchronize()
+        assert np.array_equal(xd.cpu().numpy(), y)
+
+
+@pytest.mark.parametrize("n", [3000, 1024])
+def test_config2_r2c_c2r_batch4096_device(n):
+    g = torch.Generator().manual_seed(12345)
+    b = 4096
+    x = torch.randn((b, n), generator=g)
+    xd = x.to(_dev())
+    Xd = torch.empty((b, n // 2 + 1), dtype=torch.complex64, device=_dev())
+    yd = torch.empty((b, n), device=_dev())
+    with A.Plan.plan1d(n, A.R2C, b) as pr, A.Plan.plan1d(n, A.C2R, b) as pc:
+        pr.set_stream(torch.cuda.current_stream())
+        pc.set_stream(torch.cuda.current_stream())
+        pr.exec_r2c(xd, Xd)
+        pc.exec_c2r(Xd, yd)
+        torch.cuda.synchronize()
+        X = Xd.cpu().numpy()
+        _fp64_ok(X, O.r2c(x.numpy()), what=f"r2c {n}")
+        _fp64_ok(yd.cpu().numpy(), O.c2r(X, n), what=f"c2r {n}")
+        _fp64_ok(yd.cpu().numpy(), n * x.numpy().astype(np.float64), what=f"round trip {n}")
+
+
+@pytest.mark.parametrize("n", [65536, 16384])
+def test_config3_c2c_batch64_device(n):
+    g = torch.Generator().manual_seed(12345)
+    x = _normal_c64(g, (64, n))
+    xd = x.to(_dev())
+    yd = torch.empty_like(xd)
+    with A.Plan.plan1d(n, A.C2C, 64) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2c(xd, yd, A.FORWARD)
+        torch.cuda.synchronize()
+        e = _fp64_ok(yd.cpu().numpy(), O.c2c(x.numpy(), -1), what=f"cfg3 {n}")
+        assert e["rel_l2"] < 2e-6
+        # in place (uses the plan's workspace routing)
+        zd = xd.clone()
+        p.exec_c2c(zd, zd, A.FORWARD)
+        torch.cuda.synchronize()
+        assert torch.equal(zd, yd)
+
+
+def test_config4_2d_2048_batch8_forward_inverse():
+    g = torch.Generator().manual_seed(12345)
+    x = _uniform_c64(g, (8, 2048, 2048))
+    xd = x.to(_dev())
+    yd = torch.empty_like(xd)
+    zd = torch.empty_like(xd)
+    with A.Plan.plan2d(8, 2048, 2048, A.C2C) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2c(xd, yd, A.FORWARD)
+        p.set_norm(A.NORM_BACKWARD)  # inverse scaled by 1/(2048*2048)
+        p.exec_c2c(yd, zd, A.BACKWARD)
+        torch.cuda.synchronize()
+        _fp64_ok(yd[0].cpu().numpy(), O.c2c_2d(x[0].numpy(), -1), what="2d fwd image 0")
+        _fp64_ok(zd.cpu().numpy(), x.numpy(), what="2d round trip")
+
+
+# ------------------------------------------------------------- edge cases
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 11, 13, 16, 17, 30, 47, 64, 100, 121, 143, 210, 256, 420, 1000,
+                               1536, 2048, 2310, 4096, 6561, 8192, 12288, 13312, 16384, 32768, 46200, 100000])
+def test_c2c_lengths_both_directions(n):
+    b = max(1, min(64, (1 << 20) // n))
+    rng = np.random.default_rng(n)
+    x = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
+    for d in (A.FORWARD, A.BACKWARD):
+        out = c2c_host(n, b, x.reshape(-1).copy(), d).reshape(b, n)
+        _fp64_ok(out, O.c2c(x, d), what=(n, d))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 6, 7, 8, 9, 15, 16, 30, 33, 64, 100, 255, 256, 999, 1023, 1024, 1025, 2048,
+                               3000, 5040, 8190, 12288, 25200, 26624, 32768, 65536, 100000])
+def test_r2c_c2r_lengths(n):
+    b = max(1, min(32, (1 << 20) // n))
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    X = np.empty((b, n // 2 + 1), dtype=np.complex64)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.exec_r2c(x, X)
+    _fp64_ok(X, O.r2c(x), what=("r2c", n))
+    y = np.empty((b, n), dtype=np.float32)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.exec_c2r(X, y)
+    _fp64_ok(y, O.c2r(X, n), what=("c2r", n))
+
+
+def test_delta_inputs_pin_index_maps():
+    """x = e_m gives X[k] = W^{mk}: any index-permutation error in any pass
+    shows up as an O(1) error, so this pins the index maps exactly."""
+    for n in (4096, 1500, 65536, 46200):
+        ms = [0, 1, 7, n // 2, n - 1]
+        x = np.zeros((len(ms), n), dtype=np.complex64)
+        for r, m in enumerate(ms):
+            x[r, m] = 1.0
+        out = c2c_host(n, len(ms), x.reshape(-1).copy(), A.FORWARD).reshape(len(ms), n)
+        k = np.arange(n)
+        for r, m in enumerate(ms):
+            exact = np.exp(-2j * np.pi * ((m * k) % n) / n)
+            assert np.abs(out[r] - exact).max() < 2e-6, (n, m)
+
+
+def test_vertical_large_and_inplace_device():
+    for n, b in ((256, 128), (4096, 128), (262144, 4)):
+        rng = np.random.default_rng(n)
+        x = (rng.standard_normal((n, b)) + 1j * rng.standard_normal((n, b))).astype(np.complex64)
+        xd = torch.from_numpy(x).to(_dev())
+        with A.Plan.plan1d(n, A.C2C, b, A.VERTICAL) as p:
+            p.set_stream(torch.cuda.current_stream())
+            p.exec_c2c(xd, xd, A.BACKWARD)
+            torch.cuda.synchronize()
+        _fp64_ok(xd.cpu().numpy(), O.c2c_vertical(x, +1), what=("vertical", n))
+
+
+@pytest.mark.parametrize("n", [1024, 3000, 7, 65536])
+def test_r2c_c2r_inplace_device(n):
+    b = 8
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    buf = torch.zeros(b * (n // 2 + 1) * 2, device=_dev())
+    buf[: b * n] = torch.from_numpy(x.reshape(-1)).to(_dev())
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_r2c(buf, buf)
+    torch.cuda.synchronize()
+    X = buf.cpu().numpy().view(np.complex64).reshape(b, n // 2 + 1)
+    _fp64_ok(X, O.r2c(x), what=("r2c in place", n))
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2r(buf, buf)
+    torch.cuda.synchronize()
+    y = buf.cpu().numpy()[: b * n].reshape(b, n)
+    _fp64_ok(y, n * x.astype(np.float64), what=("c2r in place", n))
+
+
+@pytest.mark.parametrize("mode", [A.NORM_NONE, A.NORM_BACKWARD, A.NORM_ORTHO, A.NORM_FORWARD])
+def test_norm_modes(mode):
+    n, b = 1000, 3
+    rng = np.random.default_rng(mode)
+    x = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
+    sf = {A.NORM_NONE: 1, A.NORM_BACKWARD: 1, A.NORM_ORTHO: n ** -0.5, A.NORM_FORWARD: 1 / n}[mode]
+    sb = {A.NORM_NONE: 1, A.NORM_BACKWARD: 1 / n, A.NORM_ORTHO: n ** -0.5, A.NORM_FORWARD: 1}[mode]
+    with A.Plan.plan1d(n, A.C2C, b) as p:
+        p.set_norm(mode)
+        f = np.empty_like(x)
+        p.exec_c2c(x, f, A.FORWARD)
+        bk = np.empty_like(x)
+        p.exec_c2c(x, bk, A.BACKWARD)
+    _fp64_ok(f, sf * O.c2c(x, -1), what="fwd")
+    _fp64_ok(bk, sb * O.c2c(x, +1), what="bwd")
+
+
+def test_unsupported_length_is_not_implemented_on_gpu():
+    n = 53 * 7
+    x = np.zeros(n, dtype=np.complex64)
+    with A.Plan.plan1d(n, A.C2C, 1) as p:
+        assert A.lib().aclfftExecC2C(p.handle, x.ctypes.data, x.ctypes.data, -1) == A.NOT_IMPLEMENTED
+
+
+# -------------------------------------------------------------- adjoints
+def _fd_grad(f, x, h=1e-6):
+    """Central finite differences of a real scalar f over a real vector x."""
+    g = np.zeros_like(x)
+    for i in range(x.size):
+        e = np.zeros_like(x)
+        e.flat[i] = h
+        g.flat[i] = (f(x + e) - f(x - e)) / (2 * h)
+    return g
+
+
+def test_adjoint_c2c_against_fd():
+    n, b = 64, 4
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))
+    G = rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))
+    for d in (A.FORWARD, A.BACKWARD):
+        # L(x) = sum Re(conj(G) * F_d(x)); complex gradient dL/dRe + i dL/dIm
+        def L(v):
+            z = v[: v.size // 2] + 1j * v[v.size // 2:]
+            return float(np.sum(np.real(np.conj(G) * O.c2c(z.reshape(b, n), d))))
+        v0 = np.concatenate([x.real.reshape(-1), x.imag.reshape(-1)])
+        gfd = _fd_grad(L, v0)
+        gfd = gfd[: v0.size // 2] + 1j * gfd[v0.size // 2:]
+        out = np.empty((b, n), dtype=np.complex64)
+        with A.Plan.plan1d(n, A.C2C, b) as p:
+            p.exec_c2c_adjoint(G.astype(np.complex64), out, d)
+        _fp64_ok(out.reshape(-1), gfd, bound=1e-5, what=("c2c adjoint", d))
+
+
+@pytest.mark.parametrize("n", [64, 63])
+def test_adjoint_r2c_against_fd_and_torch(n):
+    b = 4
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((b, n))
+    w = rng.uniform(0, 1, (b, n // 2 + 1))
+
+    def L(v):
+        X = O.r2c(v.reshape(b, n))
+        return float(np.sum(w * np.abs(X) ** 2))
+
+    gfd = _fd_grad(L, x.reshape(-1)).reshape(b, n)
+    Xbar = (2 * w * O.r2c(x)).astype(np.complex64)  # dL/dX in the complex-gradient convention
+    out = np.empty((b, n), dtype=np.float32)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.exec_r2c_adjoint(Xbar, out)
+    _fp64_ok(out, gfd, bound=1e-5, what="r2c adjoint vs FD")
+    xt = torch.tensor(x, dtype=torch.float64, requires_grad=True)
+    Lt = (torch.tensor(w) * torch.fft.rfft(xt).abs() ** 2).sum()
+    Lt.backward()
+    _fp64_ok(out, xt.grad.numpy(), bound=1e-5, what="r2c adjoint vs torch")
+
+
+@pytest.mark.parametrize("n", [64, 63])
+def test_adjoint_c2r_against_fd_and_torch(n):
+    b = 4
+    nb = n // 2 + 1
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((b, nb)) + 1j * rng.standard_normal((b, nb))
+    v = rng.standard_normal((b, n))
+
+    def L(u):
+        Z = u[: u.size // 2] + 1j * u[u.size // 2:]
+        return float(np.sum(v * O.c2r(Z.reshape(b, nb), n)))
+
+    u0 = np.concatenate([X.real.reshape(-1), X.imag.reshape(-1)])
+    g = _fd_grad(L, u0)
+    gfd = (g[: u0.size // 2] + 1j * g[u0.size // 2:]).reshape(b, nb)
+    out = np.empty((b, nb), dtype=np.complex64)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.exec_c2r_adjoint(v.astype(np.float32), out)
+    _fp64_ok(out, gfd, bound=1e-5, what="c2r adjoint vs FD")
+    Xt = torch.tensor(X, dtype=torch.complex128, requires_grad=True)
+    Lt = (torch.tensor(v) * torch.fft.irfft(Xt, n=n) * n).sum()
+    Lt.backward()
+    # torch's irfft gradient follows the same Hermitian convention
+    _fp64_ok(out, Xt.grad.numpy(), bound=1e-5, what="c2r adjoint vs torch")
+
+
+def test_twiddles_are_correctly_rounded_fp64_values():
+    """The GPU-generated FP32 twiddles equal the FP64 unit roots rounded to
+    FP32 (a 1-ulp allowance covers double-rounding ties)."""
+    with A.Plan.plan1d(4096, A.C2C, 1) as p:
+        tw = p.twiddles()
+    assert tw.size > 0
+    mag = np.abs(tw.astype(np.complex128))
+    assert np.abs(mag - 1).max() < 2e-7

@@ -1,0 +1,124 @@
+"""CPU tests of the oracle itself: it must reproduce the reference's golden
+vectors (pinning) before anything is checked against it."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import as_complex, cases, read_bin
+
+# Tight bound for the FP64 oracle against the float32 goldens: the goldens
+# are torch.fft complex64 results, so they carry float32 rounding (~1e-7).
+GOLD_REL = 2e-6
+
+
+def _check_gold(out, gold, c):
+    ok, det = O.comparison_details(out, gold, c["atol"], c["rtol"])
+    assert ok, det
+    assert det["rel_l2"] < GOLD_REL, det
+
+
+@pytest.mark.parametrize("c", cases("fft1_d"), ids=lambda c: c["name"])
+def test_oracle_pins_fft1_d(c):
+    n, b = c["n"], c["batch"]
+    x = as_complex(read_bin("fft1_d", c["files"]["input"]))
+    gold = read_bin("fft1_d", c["files"]["golden"])
+    if c.get("roundtrip"):
+        fwd = O.c2c(x.reshape(b, n), -1)
+        gfwd = read_bin("fft1_d", c["files"]["golden_forward"])
+        _check_gold(fwd, gfwd, c)
+        out = O.c2c(fwd, +1)
+    elif c.get("vertical"):
+        out = O.c2c_vertical(x.reshape(n, b), -1 if c["forward"] else +1)
+    else:
+        out = O.c2c(x.reshape(b, n), -1 if c["forward"] else +1)
+    _check_gold(out, gold, c)
+
+
+@pytest.mark.parametrize("c", cases("rfft1_d"), ids=lambda c: c["name"])
+def test_oracle_pins_rfft1_d(c):
+    n, b = c["n"], c["batch"]
+    x = read_bin("rfft1_d", c["files"]["input"]).reshape(b, n)
+    gold = read_bin("rfft1_d", c["files"]["golden"])
+    _check_gold(O.r2c(x), gold, c)
+
+
+@pytest.mark.parametrize("c", cases("irfft1_d"), ids=lambda c: c["name"])
+def test_oracle_pins_irfft1_d(c):
+    n, b = c["n"], c["batch"]
+    X = as_complex(read_bin("irfft1_d", c["files"]["input"])).reshape(b, n // 2 + 1)
+    gold = read_bin("irfft1_d", c["files"]["golden"])
+    _check_gold(O.c2r(X, n), gold, c)
+
+
+@pytest.mark.parametrize("c", cases("fft2_d"), ids=lambda c: c["name"])
+def test_oracle_pins_fft2_d(c):
+    nx, ny, b = c["fft_x"], c["fft_y"], c["batch"]
+    x = as_complex(read_bin("fft2_d", c["files"]["input"])).reshape(b, nx, ny)
+    gold = read_bin("fft2_d", c["files"]["golden"])
+    _check_gold(O.c2c_2d(x, -1 if c["forward"] else +1), gold, c)
+
+
+def test_known_answer_n2():
+    """N=2 example of the reference's test guide: {1+2j, 3+4j} -> {4+6j, -2-2j}."""
+    out = O.c2c(np.array([[1 + 2j, 3 + 4j]]), -1)
+    assert np.array_equal(out, np.array([[4 + 6j, -2 - 2j]]))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 12, 97, 210, 1000, 4096, 4099])
+def test_oracle_against_direct_dft(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    bins = np.unique(np.array([0, 1, n // 3, n // 2, n - 1]) % n)
+    for sign in (-1, 1):
+        full = O.c2c(x[None], sign)[0]
+        direct = O.dft_bins(x, bins, sign)
+        assert np.abs(full[bins] - direct).max() <= 1e-12 * max(1.0, np.abs(direct).max()) * n
+
+
+@pytest.mark.parametrize("n", [1, 2, 6, 7, 8, 15, 64, 1000, 1023, 3000])
+def test_real_oracles_consistent_with_complex(n):
+    rng = np.random.default_rng(n + 7)
+    x = rng.standard_normal((3, n))
+    X = O.r2c(x)
+    full = O.c2c(x.astype(np.complex128), -1)
+    assert np.abs(X - full[:, : n // 2 + 1]).max() < 1e-11 * n
+    y = O.c2r(X, n)
+    assert np.abs(y - n * x).max() < 1e-10 * n
+
+
+def test_port_matches_oracle():
+    """The FP32 port of the reference path used as the CPU baseline."""
+    rng = np.random.default_rng(3)
+    for n in (64, 1500, 3000, 1024):
+        x = rng.standard_normal((4, n)).astype(np.float32)
+        e = O.errors(O.port_r2c(x), O.r2c(x))
+        assert e["rel_l2"] < 1e-5, (n, e)
+        X = O.r2c(x)
+        e = O.errors(O.port_c2r(X.astype(np.complex64), n), O.c2r(X, n))
+        assert e["rel_l2"] < 1e-5, (n, e)
+    z = (rng.standard_normal((2, 4096)) + 1j * rng.standard_normal((2, 4096))).astype(np.complex64)
+    assert O.errors(O.port_c2c(z), O.c2c(z))["rel_l2"] < 1e-5
+
+
+def test_ordered_factorize_matches_reference_examples():
+    # examples verified against the reference's own helper
+    assert O.ordered_factorize(4096) == [2] * 12
+    assert O.ordered_factorize(3000) == [2, 2, 2, 3, 5, 5, 5]
+    assert O.ordered_factorize(46200) == [2, 2, 2, 3, 5, 5, 7, 11]
+    assert O.choose_radix(True, 4096) == 2
+    assert O.choose_radix(True, 3000) == -2
+    assert O.choose_radix(False, 4096) == -2
+    assert O.choose_radix(True, 53 * 2) == -1
+
+
+@pytest.mark.parametrize("radices", [[2], [4, 4], [16, 16, 16], [15, 10, 10], [8, 8, 8], [11, 5, 4], [37, 9, 3], [7, 2, 3]])
+def test_stockham_index_maps_are_permutations(radices):
+    """Each pass's read and write maps cover [0, L) exactly once (integers,
+    bit-exact), and the passes compose to a natural-order DFT."""
+    L = int(np.prod(radices))
+    for read, write in O.stockham_index_maps(radices):
+        assert np.array_equal(np.sort(read.reshape(-1)), np.arange(L))
+        assert np.array_equal(np.sort(write.reshape(-1)), np.arange(L))
+    rng = np.random.default_rng(L)
+    x = rng.standard_normal(L) + 1j * rng.standard_normal(L)
+    assert np.abs(O.stockham_simulate_exact(x, radices) - O.c2c(x[None])[0]).max() < 1e-10 * L
