@@ -44,26 +44,39 @@ enum WeightMode : int32_t {
     WEIGHT_LOAD_HALF = 2,  // multiply interior input bins by 1/2 (R2C adjoint)
 };
 
-// Contiguous transforms, one on-chip transform per batch item.
+// Contiguous transforms, one on-chip transform per batch item.  The row
+// kernel is persistent: CTA b handles tiles b, b + grid, ... of `tfpc`
+// consecutive transforms; the raw input of upcoming tiles is prefetched into
+// `nstage` shared stage buffers with bulk asynchronous copies.
 struct RowArgs {
     InnerPlan ip;
-    const void* tw;       // float2 pass tables
+    const void* tw;       // float2 twiddle blob (device)
     const void* post_tw;  // float2 W_N^k for k <= L/2 (even R2C/C2R), N = 2L
     const void* in;
     void* out;
+    int* err;             // device error word (bounded waits that timed out)
     int64_t ntf;       // number of transforms
     int64_t in_dist;   // distance between transforms, in elements of the input type
     int64_t out_dist;  // same for the output
-    int32_t tfpc;      // transforms per CTA
-    int32_t lpad;      // float2 pitch of one shared buffer
-    int32_t nbuf;      // shared buffers per transform (1 or 2)
+    int32_t tfpc;      // transforms per tile (per CTA iteration)
+    int32_t lpad;      // float2 pitch of one shared work buffer
+    int32_t nbuf;      // shared work buffers per transform (1 or 2)
     int32_t io_mode;
     int32_t conj_in;   // conjugate on load (backward transforms)
     int32_t conj_out;  // conjugate on store
     int32_t weight;
     int32_t nreal;     // N for the real-data modes
-    int32_t staged;    // cooperative contiguous copies through shared memory
+    int32_t staged;    // write results through shared memory (small transforms)
     float scale;
+    int32_t nstage;    // input stage buffers
+    int32_t pshift;    // shared padding: index i is stored at i + (i >> pshift)
+    int32_t in_esize;  // bytes per input element: 4 (real) or 8 (complex)
+    int32_t tw_lo;     // first float2 of the pass tables in the blob
+    int32_t tw_cnt;    // float2 entries of the pass tables copied to shared memory
+    int32_t post_cnt;  // post-process twiddles copied to shared memory
+    int32_t stage_bytes;
+    int32_t smem_tw, smem_post, smem_stage, smem_work, smem_bytes;  // byte offsets / total
+    int32_t grid;      // persistent CTAs
 };
 
 // Strided ("column") transforms, optionally one outer Stockham pass of a
@@ -91,6 +104,7 @@ struct ColArgs {
     int32_t tfpc;      // columns per CTA
     int32_t tfp;       // shared-memory pitch in columns (>= tfpc)
     int32_t nbuf;      // shared buffers (1 or 2), each L*tfp float2
+    int32_t pad_;
     int32_t conj_in;
     int32_t conj_out;
     int32_t staged_out;  // output of column c is out + c*L + k (contiguous blocks)

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "row_pipe.cuh"
 #include "stockham.cuh"
 
 namespace gfft {
@@ -21,19 +22,41 @@ inline cudaError_t ensure_smem_attr(K kernel, unsigned long long& done_mask, siz
     return e;
 }
 
+inline int sm_count()
+{
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    int& c = cached[dev & 63];
+    if (c == 0 && cudaDeviceGetAttribute(&c, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) c = 0;
+    return c;
+}
+
 template <int RMAX>
 int launch_row_t(const RowArgs* a, cudaStream_t st)
 {
     static unsigned long long attr_mask = 0;
+    static thread_local int last_threads = -1, last_smem = -1, last_occ = 1;
     const int threads = a->ip.nthr * a->tfpc;
     if (threads <= 0 || threads > kernel_max_threads<RMAX>() || a->ntf <= 0) return (int)cudaErrorInvalidValue;
-    const size_t smem = (size_t)a->tfpc * (size_t)a->nbuf * (size_t)a->lpad * sizeof(float2);
-    if (smem > (size_t)kMaxSmemBytes) return (int)cudaErrorInvalidValue;
-    cudaError_t e = ensure_smem_attr(row_kernel<RMAX>, attr_mask, smem);
+    if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
+        return (int)cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(row_kernel<RMAX>, attr_mask, (size_t)a->smem_bytes);
     if (e != cudaSuccess) return (int)e;
-    const int64_t grid = (a->ntf + a->tfpc - 1) / a->tfpc;
-    if (grid > 0x7fffffff) return (int)cudaErrorInvalidValue;
-    row_kernel<RMAX><<<(unsigned)grid, threads, smem, st>>>(*a);
+    if (threads != last_threads || a->smem_bytes != last_smem) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, row_kernel<RMAX>, threads, (size_t)a->smem_bytes);
+        if (e != cudaSuccess) return (int)e;
+        last_threads = threads;
+        last_smem = a->smem_bytes;
+        last_occ = occ < 1 ? 1 : occ;
+    }
+    const int64_t ntiles = (a->ntf + a->tfpc - 1) / a->tfpc;
+    int64_t grid = (int64_t)sm_count() * last_occ;
+    if (a->grid > 0) grid = a->grid;
+    if (grid < 1) grid = 1;
+    if (grid > ntiles) grid = ntiles;
+    row_kernel<RMAX><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
     return (int)cudaGetLastError();
 }
 

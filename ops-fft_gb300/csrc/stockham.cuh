@@ -126,10 +126,12 @@ __device__ __forceinline__ void stockham_pass(const Ctx& c, const PassDesc& pd, 
 // when `last_global` the final pass writes HBM, otherwise the result ends in
 // the shared buffer that is returned (1 or 2).
 template <int RMAX, class Ctx>
-__device__ __forceinline__ int run_passes(const Ctx& c, const InnerPlan& ip, int start, bool last_global)
+__device__ __forceinline__ int run_passes(const Ctx& c, const InnerPlan& ip, int start, bool last_global,
+                                          int p_begin = 0, int p_end = kMaxPass)
 {
     int cur = start;
-    for (int p = 0; p < ip.npass; ++p) {
+    const int pe = p_end < ip.npass ? p_end : ip.npass;
+    for (int p = p_begin; p < pe; ++p) {
         const PassDesc pd = ip.pass[p];
         const int src = cur;
         const int dst = (last_global && p == ip.npass - 1) ? 0 : (cur == 1 ? 2 : 1);
@@ -168,230 +170,10 @@ __device__ __forceinline__ int run_passes(const Ctx& c, const InnerPlan& ip, int
 }
 #undef GFFT_RADIX_CASE
 
-// ============================================================ row kernel
-struct RowCtx {
-    int L, nthr, tid;
-    bool ok_sm, ok_io;
-    const float2* tw;
-    float2* sA;
-    float2* sB;
-    // HBM access of the current transform
-    const float2* in2;
-    const float* in1;
-    float2* out2;
-    float* out1;
-    int mode, conj_in, conj_out, weight, nreal;
-    float scale;
-
-    __device__ __forceinline__ float2* buf(int b) const { return b == 1 ? sA : sB; }
-    __device__ __forceinline__ float2 sget(int b, int i) const { return buf(b)[spad(i)]; }
-    __device__ __forceinline__ void sput(int b, int i, float2 x) const { buf(b)[spad(i)] = x; }
-
-    __device__ __forceinline__ float2 gload(int i) const
-    {
-        if (mode == IO_R2C_ODD) return make_float2(__ldg(in1 + i), 0.f);
-        if (mode == IO_C2R_ODD) {
-            // Hermitian expansion of bins 0..N/2 to N bins, conjugated for the
-            // backward-as-forward trick; interior bins optionally halved.
-            const int h = nreal >> 1;
-            float2 x = (i <= h) ? ldg2(in2 + i) : cconj(ldg2(in2 + (nreal - i)));
-            if (weight == WEIGHT_LOAD_HALF && i != 0) x = cscale(x, 0.5f);
-            return cconj(x);
-        }
-        float2 x = ldg2(in2 + i);
-        return conj_in ? cconj(x) : x;
-    }
-    __device__ __forceinline__ void gstore(int i, float2 x) const
-    {
-        if (mode == IO_R2C_ODD) {
-            if (i <= (nreal >> 1)) {
-                float sc = scale;
-                if (weight == WEIGHT_STORE_X2 && i != 0) sc *= 2.f;
-                out2[i] = cscale(x, sc);
-            }
-            return;
-        }
-        if (mode == IO_C2R_ODD) {
-            out1[i] = x.x * scale;  // Re(conj(x)) == Re(x)
-            return;
-        }
-        if (conj_out) x = cconj(x);
-        out2[i] = cscale(x, scale);
-    }
-};
-
-// Cooperative copy of `rows` rows of `len` float2 (global stride `dist`)
-// into padded shared rows (row r at sm + r*pitch).
-__device__ __forceinline__ void copy_rows_in(float2* sm, int pitch, const float2* g, int64_t dist, int rows, int len,
-                                             bool conj)
-{
-    const int total = rows * len;
-    const float inv = 1.0f / (float)len;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int r = fdivf(e, inv);
-        const int i = e - r * len;
-        float2 x = ldg2(g + (int64_t)r * dist + i);
-        sm[r * pitch + spad(i)] = conj ? cconj(x) : x;
-    }
-}
-
-__device__ __forceinline__ void copy_rows_out(const float2* sm, int pitch, float2* g, int64_t dist, int rows, int len,
-                                              bool conj, float scale)
-{
-    const int total = rows * len;
-    const float inv = 1.0f / (float)len;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int r = fdivf(e, inv);
-        const int i = e - r * len;
-        float2 x = sm[r * pitch + spad(i)];
-        if (conj) x = cconj(x);
-        g[(int64_t)r * dist + i] = cscale(x, scale);
-    }
-}
-
-// Shared-memory layout: transform tl owns [tl*pitch, (tl+1)*pitch) with
-// pitch = nbuf*lpad; buffer A at +0 and buffer B at +lpad.
-template <int RMAX>
-__device__ __forceinline__ void row_body(const RowArgs& A)
-{
-    extern __shared__ float2 smem[];
-    const int nthr = A.ip.nthr;
-    const int tl = threadIdx.x / nthr;
-    const int tid = threadIdx.x - tl * nthr;
-    const int64_t t0 = (int64_t)blockIdx.x * A.tfpc;
-    const int64_t t = t0 + tl;
-    const int nrows = (int)min((int64_t)A.tfpc, A.ntf - t0);
-    const int pitch = A.nbuf * A.lpad;
-
-    RowCtx c;
-    c.L = A.ip.L;
-    c.nthr = nthr;
-    c.tid = tid;
-    c.ok_sm = tl < A.tfpc;
-    c.ok_io = c.ok_sm && t < A.ntf;
-    c.tw = reinterpret_cast<const float2*>(A.tw);
-    c.sA = smem + (c.ok_sm ? tl : 0) * pitch;
-    c.sB = c.sA + A.lpad;
-    c.mode = A.io_mode;
-    c.conj_in = A.conj_in;
-    c.conj_out = A.conj_out;
-    c.weight = A.weight;
-    c.nreal = A.nreal;
-    c.scale = A.scale;
-    const int64_t tt = c.ok_io ? t : 0;
-    c.in2 = reinterpret_cast<const float2*>(A.in) + tt * A.in_dist;
-    c.in1 = reinterpret_cast<const float*>(A.in) + tt * A.in_dist;
-    c.out2 = reinterpret_cast<float2*>(A.out) + tt * A.out_dist;
-    c.out1 = reinterpret_cast<float*>(A.out) + tt * A.out_dist;
-
-    const int L = c.L;
-    const float2* post = reinterpret_cast<const float2*>(A.post_tw);
-
-    int start = 0;
-    bool last_global = true;
-    if (A.io_mode == IO_C2C && A.staged) {
-        copy_rows_in(smem, pitch, reinterpret_cast<const float2*>(A.in) + t0 * A.in_dist, A.in_dist, nrows, L,
-                     A.conj_in != 0);
-        __syncthreads();
-        start = 1;
-        last_global = false;
-    } else if (A.io_mode == IO_R2C_EVEN) {
-        last_global = false;  // the post-process needs Z[k] and Z[L-k]
-        if (A.staged) {
-            copy_rows_in(smem, pitch, reinterpret_cast<const float2*>(A.in) + t0 * A.in_dist, A.in_dist, nrows, L,
-                         false);
-            __syncthreads();
-            start = 1;
-        }
-    } else if (A.io_mode == IO_C2R_EVEN) {
-        start = 1;
-        // bins 0..L into buffer A
-        if (A.staged) {
-            copy_rows_in(smem, pitch, reinterpret_cast<const float2*>(A.in) + t0 * A.in_dist, A.in_dist, nrows, L + 1,
-                         false);
-        } else if (c.ok_io) {
-            for (int k = tid; k <= L; k += nthr) c.sput(1, k, ldg2(c.in2 + k));
-        }
-        __syncthreads();
-        // pre-process pairs (k, L-k):  Z'[k] = E + i*O with
-        //   E = X[k] + conj(X[L-k]),  O = (X[k] - conj(X[L-k])) * conj(W_N^k)
-        // stored conjugated (backward transform as conj of a forward one).
-        if (c.ok_sm) {
-            const bool half = A.weight == WEIGHT_LOAD_HALF;
-            for (int k = tid; k <= (L >> 1); k += nthr) {
-                if (k == 0) {
-                    const float x0 = c.sget(1, 0).x, xl = c.sget(1, L).x;
-                    const float e = x0 + xl, o = x0 - xl;  // imaginary parts of DC/Nyquist are ignored
-                    c.sput(1, 0, make_float2(e, -o));
-                } else {
-                    float2 a = c.sget(1, k), b = c.sget(1, L - k);
-                    if (half) {
-                        a = cscale(a, 0.5f);
-                        b = cscale(b, 0.5f);
-                    }
-                    const float2 w = ldg2(post + k);  // W_N^k
-                    const float2 bc = cconj(b);
-                    const float2 e = cadd(a, bc);
-                    const float2 o = cmulc(csub(a, bc), w);  // * conj(W_N^k)
-                    const float2 zk = make_float2(e.x - o.y, e.y + o.x);   // e + i*o
-                    const float2 zl = make_float2(e.x + o.y, -e.y + o.x);  // conj(e) + i*conj(o)
-                    c.sput(1, k, cconj(zk));
-                    if (L - k != k) c.sput(1, L - k, cconj(zl));
-                }
-            }
-        }
-        __syncthreads();
-    }
-
-    const int fin = run_passes<RMAX>(c, A.ip, start, last_global);
-
-    if (A.io_mode == IO_C2C && A.staged) {
-        copy_rows_out(smem + (fin == 2 ? A.lpad : 0), pitch, reinterpret_cast<float2*>(A.out) + t0 * A.out_dist,
-                      A.out_dist, nrows, L, A.conj_out != 0, A.scale);
-    } else if (A.io_mode == IO_R2C_EVEN) {
-        // post-process pairs in shared memory:
-        //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
-        //   X[k] = E + W^k O,  X[L-k] = conj(E - W^k O),
-        //   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0 (zero imaginary parts)
-        if (c.ok_sm) {
-            const bool x2 = A.weight == WEIGHT_STORE_X2;
-            const float sc = A.scale;
-            const float s2 = x2 ? 2.f * sc : sc;
-            for (int k = tid; k <= (L >> 1); k += nthr) {
-                if (k == 0) {
-                    const float2 z0 = c.sget(fin, 0);
-                    c.sput(fin, 0, make_float2((z0.x + z0.y) * sc, 0.f));
-                    c.sput(fin, L, make_float2((z0.x - z0.y) * sc, 0.f));
-                } else {
-                    const float2 zk = c.sget(fin, k), zc = cconj(c.sget(fin, L - k));
-                    const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
-                    const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
-                    const float2 wo = cmul(ldg2(post + k), o);
-                    c.sput(fin, k, cscale(cadd(e, wo), s2));
-                    if (L - k != k) c.sput(fin, L - k, cscale(cconj(csub(e, wo)), s2));
-                }
-            }
-        }
-        __syncthreads();
-        if (A.staged) {
-            copy_rows_out(smem + (fin == 2 ? A.lpad : 0), pitch, reinterpret_cast<float2*>(A.out) + t0 * A.out_dist,
-                          A.out_dist, nrows, L + 1, false, 1.f);
-        } else if (c.ok_io) {
-            for (int k = tid; k <= L; k += nthr) c.out2[k] = c.sget(fin, k);
-        }
-    }
-}
-
 template <int RMAX>
 constexpr int kernel_max_threads()
 {
     return RMAX <= 16 ? 512 : 256;
-}
-
-template <int RMAX>
-__global__ void __launch_bounds__(kernel_max_threads<RMAX>()) row_kernel(const __grid_constant__ RowArgs A)
-{
-    row_body<RMAX>(A);
 }
 
 // ========================================================= column kernel

@@ -70,6 +70,7 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
             s.row.post_tw = s.post_off >= 0 ? tw + s.post_off : nullptr;
             s.row.in = src;
             s.row.out = dst;
+            s.row.err = impl->err;
             if (c2c) {
                 s.row.conj_in = first && inverse;
                 s.row.conj_out = last && inverse;

@@ -138,6 +138,8 @@ void plan_impl_free(PlanImpl* p)
     if (p->ws2) cudaFree(p->ws2);
     if (p->stage_a) cudaFree(p->stage_a);
     if (p->stage_b) cudaFree(p->stage_b);
+    if (p->err) cudaFree(p->err);
+    p->err = nullptr;
     p->tw = p->ws = p->ws2 = p->stage_a = p->stage_b = nullptr;
     p->device_ready = false;
 }
@@ -177,6 +179,13 @@ aclfftResult plan_device_setup(PlanImpl* p)
         p->ws2 = nullptr;
         plan_impl_free(p);
         set_last_error("cudaMalloc of the second workspace failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    if (cudaMalloc(reinterpret_cast<void**>(&p->err), sizeof(int)) != cudaSuccess || cudaMemset(p->err, 0, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        p->err = nullptr;
+        plan_impl_free(p);
+        set_last_error("cudaMalloc of the error word failed");
         return ACLFFT_ALLOC_FAILED;
     }
     if (!p->tb.segs.empty()) {

@@ -32,6 +32,7 @@ struct PlanImpl {
     void* tw = nullptr;
     void* ws = nullptr;
     void* ws2 = nullptr;
+    int* err = nullptr;  // device error word written by bounded waits
     // host staging (allocated on the first exec with host pointers)
     void* stage_a = nullptr;
     void* stage_b = nullptr;

@@ -75,24 +75,30 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const int L = a.ip.L;
     const int maxthr = a.ip.rmax == 16 ? 512 : 256;
     if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1) return fail(why, "row threads");
-    if ((int64_t)a.tfpc * a.nbuf * a.lpad * 8 > kMaxSmemBytes) return fail(why, "row smem");
+    if (a.nstage < 1 || a.nstage > 4) return fail(why, "row stages");
     const bool even = a.io_mode == IO_R2C_EVEN || a.io_mode == IO_C2R_EVEN;
-    if (spad_host(even ? L : L - 1) >= a.lpad) return fail(why, "row lpad too small");
-    {
-        int start = 0;
-        bool last_global = true;
-        if (a.io_mode == IO_C2C && a.staged) {
-            start = 1;
-            last_global = false;
-        } else if (a.io_mode == IO_R2C_EVEN) {
-            last_global = false;
-            start = a.staged ? 1 : 0;
-        } else if (a.io_mode == IO_C2R_EVEN) {
-            start = 1;
+    const int maxidx = even ? L : L - 1;
+    if (maxidx + (maxidx >> a.pshift) >= a.lpad) return fail(why, "row lpad too small");
+    const int64_t row_bytes = a.in_dist * a.in_esize;
+    if ((int64_t)a.tfpc * row_bytes > a.stage_bytes || a.stage_bytes % 16) return fail(why, "row stage too small");
+    if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
+        a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 16 ||
+        a.smem_work < a.smem_stage + (int64_t)a.nstage * a.stage_bytes ||
+        a.smem_bytes < a.smem_work + (int64_t)a.tfpc * a.nbuf * a.lpad * 8 || a.smem_bytes > kMaxSmemBytes)
+        return fail(why, "row shared-memory layout");
+    if (a.tw_cnt > 0) {
+        for (int p = 0; p < a.ip.npass; ++p) {
+            const PassDesc& d = a.ip.pass[p];
+            if (d.ns > 1 && (d.tw_off < a.tw_lo || d.tw_off + (int64_t)d.ns * d.radix > a.tw_lo + a.tw_cnt))
+                return fail(why, "pass table outside the shared window");
         }
+        if (a.tw_lo + (int64_t)a.tw_cnt > tw_count || a.tw_lo % 2) return fail(why, "twiddle window");
+    }
+    {
+        const int start = a.io_mode == IO_C2R_EVEN ? 1 : 0;
+        const bool last_global = !(a.io_mode == IO_R2C_EVEN || (a.io_mode == IO_C2C && a.staged));
         if (buffers_used(a.ip.npass, start, last_global) > a.nbuf) return fail(why, "row needs more shared buffers");
     }
-    if ((a.ntf + a.tfpc - 1) / a.tfpc > 0x7fffffff) return fail(why, "row grid");
     if (a.staged && (int64_t)a.tfpc * (L + 1) >= (1 << 22)) return fail(why, "staged copy index range");
     int64_t in_last = 0, out_last = 0, in_es = 8, out_es = 8;
     const int N = a.nreal;
@@ -104,9 +110,11 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     case IO_C2R_ODD: in_last = N / 2; out_es = 4; out_last = N - 1; break;
     default: return fail(why, "io mode");
     }
+    if (in_es != a.in_esize || in_last + 1 != a.in_dist) return fail(why, "row input layout");
     if (((a.ntf - 1) * a.in_dist + in_last + 1) * in_es > b.bytes[s.src]) return fail(why, "row input out of bounds");
     if (((a.ntf - 1) * a.out_dist + out_last + 1) * out_es > b.bytes[s.dst]) return fail(why, "row output out of bounds");
     if (even && (s.post_off < 0 || s.post_off + L / 2 + 1 > tw_count)) return fail(why, "post twiddle out of table");
+    if (even && a.post_cnt != L / 2 + 1) return fail(why, "post twiddle count");
     return true;
 }
 

@@ -162,7 +162,8 @@ int col_max_length() { return 2048; }
 
 namespace {
 
-// One on-chip transform per contiguous batch item.
+// One on-chip transform per contiguous batch item (persistent row kernel,
+// see csrc/row_pipe.cuh for the shared-memory layout).
 bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io_mode, int nreal, int weight,
                    TwiddleBuilder& tb, Step& st)
 {
@@ -172,28 +173,75 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     const int maxthr = max_threads_for(rmax);
     const int nthr = pick_nthr(L, rad, maxthr);
     const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
-    const bool staged = nthr < 32 && (io_mode == IO_C2C || even_mode);
-    const int start = (io_mode == IO_C2R_EVEN || staged) ? 1 : 0;
-    const bool last_global = !(io_mode == IO_R2C_EVEN || staged);
-    const int nbuf = row_nbuf((int)rad.size(), start, last_global);
-    int lpad = spad_host(L) + 2;
+    const bool staged = nthr < 32 && (io_mode == IO_C2C || io_mode == IO_R2C_EVEN);
+    const int start = io_mode == IO_C2R_EVEN ? 1 : 0;
+    const bool last_global = !(io_mode == IO_R2C_EVEN || (io_mode == IO_C2C && staged));
+    const int nbuf = std::max(1, row_nbuf((int)rad.size(), start, last_global));
+    const int pshift = (rad[0] % 2 == 0) ? 4 : 30;
+    const int maxidx = even_mode ? L : L - 1;
+    int lpad = maxidx + (maxidx >> pshift) + 2;
     lpad += lpad & 1;
-    const int64_t per_tf = (int64_t)nbuf * lpad * 8;
-    if (per_tf > kMaxSmemBytes) return false;
-    int tf = std::max(1, 256 / nthr);
-    tf = std::min(tf, maxthr / nthr);
-    tf = (int)std::min<int64_t>(tf, std::max<int64_t>(1, (96 * 1024) / per_tf));
-    tf = (int)std::min<int64_t>(tf, ntf);
-    tf = std::max(tf, 1);
+    const int esize = io_mode == IO_R2C_ODD ? 4 : 8;
+    const int64_t row_bytes = in_dist * esize;
 
     st = Step{};
     st.kind = Step::ROW;
     RowArgs& a = st.row;
     if (!build_inner(L, rad, nthr, tb, a.ip)) return false;
+    // pass-table window (contiguous range of the blob used by this transform)
+    int64_t lo = -1, hi = -1;
+    for (int p = 0; p < a.ip.npass; ++p) {
+        const PassDesc& d = a.ip.pass[p];
+        if (d.ns <= 1) continue;
+        const int64_t b0 = d.tw_off, b1 = d.tw_off + (int64_t)d.ns * d.radix;
+        lo = lo < 0 ? b0 : std::min(lo, b0);
+        hi = std::max(hi, b1);
+    }
+    const int64_t tw_cnt = lo < 0 ? 0 : hi - lo;
+    const bool tw_in_smem = tw_cnt * 8 <= 64 * 1024;
+    const int64_t post_cnt = even_mode ? L / 2 + 1 : 0;
+    if (even_mode) st.post_off = tb.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
+
+    auto align = [](int64_t x, int64_t a) { return (x + a - 1) / a * a; };
+    const int64_t hdr = 128;
+    const int64_t tw_bytes = tw_in_smem ? align(tw_cnt * 8, 16) : 0;
+    const int64_t post_bytes = align(post_cnt * 8, 16);
+    // tiles must keep the bulk copies 16-byte aligned when rows are not
+    int tf_mult = 1;
+    while ((row_bytes * tf_mult) % 16 != 0 && tf_mult < 16) tf_mult *= 2;
+    const int64_t tmax = std::max<int64_t>(
+        1, std::min<int64_t>({(int64_t)maxthr / nthr, std::max<int64_t>(1, (48 * 1024) / row_bytes), ntf}));
+    // keep at least ~one tile per SM for small batches
+    const int64_t tcap = std::max<int64_t>(1, (ntf + 151) / 152);
+    double best = -1;
+    int best_tf = 1, best_ns = 1;
+    int64_t best_smem = 0;
+    for (int ns_ = 1; ns_ <= 3; ++ns_) {
+        for (int64_t tf = std::min(tmax, std::max<int64_t>(tcap, 1)); tf >= 1; --tf) {
+            const int64_t stage = align(tf * row_bytes, 128);
+            const int64_t work = tf * nbuf * (int64_t)lpad * 8;
+            const int64_t smem = hdr + tw_bytes + post_bytes + ns_ * stage + work;
+            if (smem > kMaxSmemBytes) continue;
+            const int64_t threads = tf * nthr;
+            const int64_t warps = (threads + 31) / 32;
+            const int64_t ctas = std::min<int64_t>({(228 * 1024) / (smem + 1024), 64 / std::max<int64_t>(warps, 1), 32});
+            if (ctas < 1) continue;
+            const double thr_sm = (double)std::min<int64_t>(ctas * threads, 1024) / 1024.0;
+            const double infl = (double)std::min<int64_t>(ctas * (ns_ - 1) * tf * row_bytes, 96 * 1024) / (96 * 1024.0);
+            double score = thr_sm + infl + (tf % tf_mult == 0 ? 0.5 : 0.0) + 0.01 * ns_;
+            if (score > best) {
+                best = score;
+                best_tf = (int)tf;
+                best_ns = ns_;
+                best_smem = smem;
+            }
+        }
+    }
+    if (best < 0) return false;
     a.ntf = ntf;
     a.in_dist = in_dist;
     a.out_dist = out_dist;
-    a.tfpc = tf;
+    a.tfpc = best_tf;
     a.lpad = lpad;
     a.nbuf = nbuf;
     a.io_mode = io_mode;
@@ -202,9 +250,21 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     a.staged = staged ? 1 : 0;
     a.scale = 1.f;
     a.conj_out = io_mode == IO_C2R_EVEN ? 1 : 0;
+    a.nstage = best_ns;
+    a.pshift = pshift;
+    a.in_esize = esize;
+    a.tw_lo = (int32_t)(lo < 0 ? 0 : lo);
+    a.tw_cnt = tw_in_smem ? (int32_t)tw_cnt : 0;
+    a.post_cnt = (int32_t)post_cnt;
+    a.stage_bytes = (int32_t)align(best_tf * row_bytes, 128);
+    a.smem_tw = (int32_t)hdr;
+    a.smem_post = (int32_t)(hdr + tw_bytes);
+    a.smem_stage = (int32_t)align(hdr + tw_bytes + post_bytes, 128);
+    a.smem_work = (int32_t)(a.smem_stage + (int64_t)best_ns * a.stage_bytes);
+    a.smem_bytes = (int32_t)(a.smem_work + (int64_t)best_tf * nbuf * lpad * 8);
+    (void)best_smem;
     st.tw_off = 0;
-    if (even_mode) st.post_off = tb.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
-    return true;
+    return a.smem_bytes <= kMaxSmemBytes;
 }
 
 // One column pass over an axis of length n (stride S between samples, S
@@ -307,17 +367,12 @@ bool make_axis_steps(int64_t n, int64_t S, int64_t items, int64_t D, int src, in
 
 bool row_feasible(int L, int io_mode)
 {
-    std::vector<int> rad = choose_radices(L);
-    if (rad.empty()) return false;
-    const int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
-    const int nthr = pick_nthr(L, rad, max_threads_for(rmax));
-    const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
-    const bool staged = nthr < 32 && (io_mode == IO_C2C || even_mode);
-    const int start = (io_mode == IO_C2R_EVEN || staged) ? 1 : 0;
-    const bool last_global = !(io_mode == IO_R2C_EVEN || staged);
-    const int nbuf = row_nbuf((int)rad.size(), start, last_global);
-    const int64_t lpad = spad_host(L) + 3;
-    return nbuf * lpad * 8 <= kMaxSmemBytes;
+    TwiddleBuilder scratch;
+    Step st;
+    const bool even = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
+    const int64_t in_dist = io_mode == IO_C2R_EVEN ? L + 1 : (io_mode == IO_C2R_ODD ? L / 2 + 1 : L);
+    const int64_t out_dist = io_mode == IO_R2C_EVEN ? L + 1 : (io_mode == IO_R2C_ODD ? L / 2 + 1 : L);
+    return make_row_step(L, 1, in_dist, out_dist, io_mode, even ? 2 * L : L, WEIGHT_NONE, scratch, st);
 }
 
 }  // namespace
