@@ -52,6 +52,8 @@ __device__ __forceinline__ int fdiv(int j, const PassDesc& pd)
 __device__ __forceinline__ int fdivf(int e, float invL) { return __float2int_rz(((float)e + 0.5f) * invL); }
 
 // --------------------------------------------------------------- one pass
+// c.tw may point to shared memory (row kernel) or global memory (column
+// kernel), so twiddles are read with generic loads.
 // Buffers: 0 = HBM (the Ctx's gload/gstore), 1 = shared buffer A,
 // 2 = shared buffer B.  Each thread walks butterflies j = tid, tid+nthr, ...
 // and streams them from the source to the destination buffer, so a pass
@@ -83,14 +85,14 @@ __device__ __forceinline__ void stockham_pass(const Ctx& c, const PassDesc& pd, 
             if constexpr (R % 2 == 0) {
                 sfor<R / 2>([&](auto hh) {
                     constexpr int h = decltype(hh)::value;
-                    const float4 ww = __ldg(reinterpret_cast<const float4*>(w) + h);
+                    const float4 ww = reinterpret_cast<const float4*>(w)[h];  // shared or global (generic load)
                     if constexpr (h > 0) u[2 * h] = cmul(u[2 * h], make_float2(ww.x, ww.y));
                     u[2 * h + 1] = cmul(u[2 * h + 1], make_float2(ww.z, ww.w));
                 });
             } else {
                 sfor<R - 1>([&](auto rr) {
                     constexpr int r = decltype(rr)::value + 1;
-                    u[r] = cmul(u[r], ldg2(w + r));
+                    u[r] = cmul(u[r], w[r]);
                 });
             }
         }
