@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "codelet_list.h"
 #include "launch_common.cuh"
 
 namespace gfft {
@@ -81,6 +82,18 @@ using namespace gfft;
 extern "C" int gfft_launch_row(const RowArgs* a, void* stream)
 {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (a->codelet) {
+    case -1: break;
+    case 0: return launch_codelet_0(a, st);
+    case 1: return launch_codelet_1(a, st);
+    case 2: return launch_codelet_2(a, st);
+    case 3: return launch_codelet_3(a, st);
+    case 4: return launch_codelet_4(a, st);
+    case 5: return launch_codelet_5(a, st);
+    case 6: return launch_codelet_6(a, st);
+    case 7: return launch_codelet_7(a, st);
+    default: return (int)cudaErrorInvalidValue;
+    }
     switch (a->ip.rmax) {
     case 16: return launch_row_r16(a, st);
     case 47: return launch_row_r47(a, st);
@@ -124,4 +137,19 @@ extern "C" int gfft_gen_twiddles(void* table, const TwSeg* segs, int nseg, void*
         if (e != cudaSuccess) return (int)e;
     }
     return 0;
+}
+
+extern "C" int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix)
+{
+#define GFFT_LOOKUP(ID, LL, NT, ...)                           \
+    if (L == LL) {                                             \
+        const int r[] = {__VA_ARGS__};                         \
+        *nthr = NT;                                            \
+        *nradix = (int)(sizeof(r) / sizeof(r[0]));             \
+        for (int i = 0; i < *nradix; ++i) radices[i] = r[i];   \
+        return ID;                                             \
+    }
+    GFFT_CODELETS(GFFT_LOOKUP)
+#undef GFFT_LOOKUP
+    return -1;
 }

@@ -76,7 +76,8 @@ struct RowArgs {
     int32_t post_cnt;  // post-process twiddles copied to shared memory
     int32_t stage_bytes;
     int32_t smem_tw, smem_post, smem_stage, smem_work, smem_bytes;  // byte offsets / total
-    int32_t grid;      // persistent CTAs
+    int32_t grid;      // persistent CTAs (0: SMs x occupancy)
+    int32_t codelet;   // compile-time specialised kernel id, -1 for the generic kernel
 };
 
 // Strided ("column") transforms, optionally one outer Stockham pass of a
@@ -145,4 +146,7 @@ int gfft_launch_col(const gfft::ColArgs* a, void* stream);
 int gfft_launch_pack(const gfft::PackArgs* a, void* stream);
 int gfft_gen_twiddles(void* table, const gfft::TwSeg* segs, int nseg, void* stream);
 int gfft_kernel_max_threads(int rmax);
+// Compile-time specialised row kernel for length L: returns its id (or -1)
+// and fills its thread count per transform and radix sequence.
+int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix);
 }

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "codelet.cuh"
 #include "row_pipe.cuh"
 #include "stockham.cuh"
 
@@ -76,6 +77,42 @@ int launch_col_t(const ColArgs* a, cudaStream_t st)
     return (int)cudaGetLastError();
 }
 
+template <class S>
+int launch_codelet_t(const RowArgs* a, cudaStream_t st)
+{
+    static unsigned long long attr_mask = 0;
+    static thread_local int last_threads = -1, last_smem = -1, last_occ = 1;
+    const int threads = S::NTHR * a->tfpc;
+    if (a->ip.L != S::L || threads <= 0 || threads > 512 || a->ntf <= 0) return (int)cudaErrorInvalidValue;
+    if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
+        return (int)cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(codelet_kernel<S>, attr_mask, (size_t)a->smem_bytes);
+    if (e != cudaSuccess) return (int)e;
+    if (threads != last_threads || a->smem_bytes != last_smem) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, codelet_kernel<S>, threads, (size_t)a->smem_bytes);
+        if (e != cudaSuccess) return (int)e;
+        last_threads = threads;
+        last_smem = a->smem_bytes;
+        last_occ = occ < 1 ? 1 : occ;
+    }
+    const int64_t ntiles = (a->ntf + a->tfpc - 1) / a->tfpc;
+    int64_t grid = (int64_t)sm_count() * last_occ;
+    if (a->grid > 0) grid = a->grid;
+    if (grid < 1) grid = 1;
+    if (grid > ntiles) grid = ntiles;
+    codelet_kernel<S><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
+    return (int)cudaGetLastError();
+}
+
+int launch_codelet_0(const RowArgs* a, cudaStream_t st);
+int launch_codelet_1(const RowArgs* a, cudaStream_t st);
+int launch_codelet_2(const RowArgs* a, cudaStream_t st);
+int launch_codelet_3(const RowArgs* a, cudaStream_t st);
+int launch_codelet_4(const RowArgs* a, cudaStream_t st);
+int launch_codelet_5(const RowArgs* a, cudaStream_t st);
+int launch_codelet_6(const RowArgs* a, cudaStream_t st);
+int launch_codelet_7(const RowArgs* a, cudaStream_t st);
 int launch_row_r16(const RowArgs* a, cudaStream_t st);
 int launch_row_r47(const RowArgs* a, cudaStream_t st);
 int launch_col_r16(const ColArgs* a, cudaStream_t st);

@@ -73,9 +73,22 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const RowArgs& a = s.row;
     if (!check_inner(a.ip, tw_count, why)) return false;
     const int L = a.ip.L;
-    const int maxthr = a.ip.rmax == 16 ? 512 : 256;
+    const int maxthr = (a.ip.rmax == 16 || a.codelet >= 0) ? 512 : 256;
     if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1) return fail(why, "row threads");
     if (a.nstage < 1 || a.nstage > 4) return fail(why, "row stages");
+    if (a.codelet >= 0) {
+        int cn = 0, cr[kMaxPass], cnr = 0;
+        if (gfft_codelet_lookup(L, &cn, cr, &cnr) != a.codelet || cn != a.ip.nthr || cnr != a.ip.npass)
+            return fail(why, "codelet mismatch");
+        for (int p = 0; p < cnr; ++p)
+            if (cr[p] != a.ip.pass[p].radix) return fail(why, "codelet radix mismatch");
+        if (a.nbuf != 1) return fail(why, "codelet buffers");
+        bool need_tw = false;
+        for (int p = 0; p < a.ip.npass; ++p) need_tw |= a.ip.pass[p].ns > 1;
+        if (need_tw && a.tw_cnt == 0) return fail(why, "codelet twiddles not in shared memory");
+        const int ps = (cr[0] % 2 == 0) ? 4 : 30;
+        if (a.pshift != ps) return fail(why, "codelet padding");
+    }
     const bool even = a.io_mode == IO_R2C_EVEN || a.io_mode == IO_C2R_EVEN;
     const int maxidx = even ? L : L - 1;
     if (maxidx + (maxidx >> a.pshift) >= a.lpad) return fail(why, "row lpad too small");
@@ -94,7 +107,7 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
         }
         if (a.tw_lo + (int64_t)a.tw_cnt > tw_count || a.tw_lo % 2) return fail(why, "twiddle window");
     }
-    {
+    if (a.codelet < 0) {
         const int start = a.io_mode == IO_C2R_EVEN ? 1 : 0;
         const bool last_global = !(a.io_mode == IO_R2C_EVEN || (a.io_mode == IO_C2C && a.staged));
         if (buffers_used(a.ip.npass, start, last_global) > a.nbuf) return fail(why, "row needs more shared buffers");

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <functional>
 
 namespace gfft {
@@ -158,6 +159,15 @@ int row_nbuf(int npass, int start, bool last_global)
 
 // Largest lengths accepted by the generic kernels (checked exactly below).
 int row_max_length() { return 13312; }
+
+bool codelets_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("OPS_FFT_CODELETS");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 int col_max_length() { return 2048; }
 
 namespace {
@@ -169,14 +179,27 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
 {
     std::vector<int> rad = choose_radices(L);
     if (rad.empty()) return false;
-    const int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
-    const int maxthr = max_threads_for(rmax);
-    const int nthr = pick_nthr(L, rad, maxthr);
+    int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
+    int maxthr = max_threads_for(rmax);
+    int nthr = pick_nthr(L, rad, maxthr);
+    // compile-time specialised kernel for this length, when one is built
+    int codelet = -1;
+    if (codelets_enabled()) {
+        int cn = 0, cr[kMaxPass], cnr = 0;
+        const int id = gfft_codelet_lookup(L, &cn, cr, &cnr);
+        if (id >= 0) {
+            codelet = id;
+            nthr = cn;
+            rad.assign(cr, cr + cnr);
+            rmax = 16;
+            maxthr = 512;
+        }
+    }
     const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
     const bool staged = nthr < 32 && (io_mode == IO_C2C || io_mode == IO_R2C_EVEN);
     const int start = io_mode == IO_C2R_EVEN ? 1 : 0;
     const bool last_global = !(io_mode == IO_R2C_EVEN || (io_mode == IO_C2C && staged));
-    const int nbuf = std::max(1, row_nbuf((int)rad.size(), start, last_global));
+    const int nbuf = codelet >= 0 ? 1 : std::max(1, row_nbuf((int)rad.size(), start, last_global));
     const int pshift = (rad[0] % 2 == 0) ? 4 : 30;
     const int maxidx = even_mode ? L : L - 1;
     int lpad = maxidx + (maxidx >> pshift) + 2;
@@ -198,7 +221,8 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
         hi = std::max(hi, b1);
     }
     const int64_t tw_cnt = lo < 0 ? 0 : hi - lo;
-    const bool tw_in_smem = tw_cnt * 8 <= 64 * 1024;
+    const bool tw_in_smem = tw_cnt * 8 <= 72 * 1024;
+    if (codelet >= 0 && !tw_in_smem) return false;  // codelets read twiddles from shared memory only
     const int64_t post_cnt = even_mode ? L / 2 + 1 : 0;
     if (even_mode) st.post_off = tb.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
 
@@ -262,6 +286,7 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     a.smem_stage = (int32_t)align(hdr + tw_bytes + post_bytes, 128);
     a.smem_work = (int32_t)(a.smem_stage + (int64_t)best_ns * a.stage_bytes);
     a.smem_bytes = (int32_t)(a.smem_work + (int64_t)best_tf * nbuf * lpad * 8);
+    a.codelet = codelet;
     (void)best_smem;
     st.tw_off = 0;
     return a.smem_bytes <= kMaxSmemBytes;

@@ -25,6 +25,9 @@ bool all_primes_at_most(int64_t n, int64_t pmax);
 int row_max_length();
 int col_max_length();
 
+// Compile-time specialised row kernels are used unless OPS_FFT_CODELETS=0.
+bool codelets_enabled();
+
 // Radix sequence for an on-chip transform of length L (product == L),
 // radices <= 16 when possible, primes up to 47 otherwise.  Empty on failure.
 std::vector<int> choose_radices(int L);
