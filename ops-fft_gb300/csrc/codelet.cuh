@@ -1,16 +1,29 @@
 // codelet.cuh - compile-time specialised row kernels ("codelets").
 //
-// Same persistent, bulk-copy-fed tile loop as row_pipe.cuh, but the length,
-// the thread count per transform and the radix sequence are template
+// The length, the threads per transform and the radix sequence are template
 // parameters, so every index, stride and twiddle-row computation folds to
-// constants and each thread keeps its butterflies in registers:
-//   * pass p: each thread owns NB_p = ceil(L/R_p / NTHR) butterflies
-//     j = tid + b*NTHR and holds their R_p inputs in registers;
-//   * passes run in place in ONE shared buffer per transform: all reads of
-//     a pass complete (barrier) before any write, so half the shared memory
-//     of the ping-pong kernel is needed;
-//   * the first pass reads the raw stage copy of the input, the last pass
-//     writes HBM directly (or shared memory for the R2C post-process).
+// constants and each thread keeps its butterflies in registers.
+//
+// Execution model (per CTA):
+//   * the CTA holds NG independent transform GROUPS of NTHR threads
+//     (NTHR a multiple of 32); groups synchronise only among themselves with
+//     a named barrier (bar.sync 1+g, NTHR), never CTA-wide, so one group's
+//     passes overlap another group's loads and stores;
+//   * each group owns a ring of NST shared SLOTS; a slot holds TPS
+//     consecutive transforms, filled by ONE bulk asynchronous copy
+//     (cp.async.bulk, completion counted on the slot's mbarrier) issued by
+//     the group leader NST slots ahead.  TPS is chosen so a slot is a 16-byte
+//     aligned, 16-byte multiple range (2 for rows of an odd number of float2);
+//   * pass p: thread owns NB_p = ceil(L/R_p / NTHR) butterflies
+//     j = tid + b*NTHR and holds their R_p inputs in registers; the passes
+//     run in place in one shared buffer per group (all reads of a pass finish
+//     before any write); the first pass reads the slot, the last pass writes
+//     HBM directly (or shared memory for the R2C post-process);
+//   * twiddle tables and the real-data post-process twiddles are copied to
+//     shared memory once per CTA.
+// Every mbarrier wait is bounded (~2 s); on expiry the group records bit 0 in
+// the plan's error word, drains its own outstanding copies (bounded) and
+// stops, leaving the context usable.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -48,6 +61,7 @@ struct CSpec {
         return n;
     }
     static_assert(product() == L, "radix product must equal L");
+    static_assert(NTHR % 32 == 0, "transform groups are whole warps");
 };
 
 template <class S>
@@ -56,11 +70,16 @@ __device__ __forceinline__ int cpad(int i)
     return i + (i >> S::PSHIFT);
 }
 
+__device__ __forceinline__ void group_sync(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
 // One in-place pass P of codelet S on the transform held in W (shared) or,
-// for P == 0 with from_stage, read from the stage copy through c.gload.
+// for P == 0 with from_slot, read from the slot copy through c.gload.
 template <class S, int P>
 __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2 (&v)[S::E], const float2* tw,
-                                             int tw_off, bool from_stage, bool last_global)
+                                             int tw_off, bool from_slot, bool last_global, int bar_id)
 {
     constexpr int R = S::R[P];
     constexpr int NS = S::ns(P);
@@ -70,50 +89,54 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
     constexpr bool LAST = P == S::NP - 1;
     const int tid = c.tid;
     // ---- load
-    if (P == 0 && from_stage) {
+    if (P == 0 && from_slot) {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
             const int j = tid + b * S::NTHR;
-            const bool act = (FULL || j < NBF) && c.ok_io;
-            sfor<R>([&](auto rr) {
-                constexpr int r = decltype(rr)::value;
-                v[b * R + r] = act ? c.gload(j + r * NBF) : make_float2(0.f, 0.f);
-            });
+            if (FULL || j < NBF) {
+                sfor<R>([&](auto rr) {
+                    constexpr int r = decltype(rr)::value;
+                    v[b * R + r] = c.gload(j + r * NBF);
+                });
+            }
         });
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
             const int j = tid + b * S::NTHR;
-            const bool act = FULL || j < NBF;
-            sfor<R>([&](auto rr) {
-                constexpr int r = decltype(rr)::value;
-                v[b * R + r] = act ? W[cpad<S>(j + r * NBF)] : make_float2(0.f, 0.f);
-            });
+            if (FULL || j < NBF) {
+                sfor<R>([&](auto rr) {
+                    constexpr int r = decltype(rr)::value;
+                    v[b * R + r] = W[cpad<S>(j + r * NBF)];
+                });
+            }
         });
-        __syncthreads();  // in place: every read of this pass precedes any write
+        group_sync(bar_id, S::NTHR);  // in place: every read of this pass precedes any write
     }
     // ---- twiddle + butterfly
     sfor<NB>([&](auto bb) {
         constexpr int b = decltype(bb)::value;
         const int j = tid + b * S::NTHR;
-        if constexpr (NS > 1) {
-            const int k = j % NS;
-            const float2* w = tw + tw_off + k * R;
-            if constexpr (R % 2 == 0) {
-                sfor<R / 2>([&](auto hh) {
-                    constexpr int h = decltype(hh)::value;
-                    const float4 ww = reinterpret_cast<const float4*>(w)[h];
-                    if constexpr (h > 0) v[b * R + 2 * h] = cmul(v[b * R + 2 * h], make_float2(ww.x, ww.y));
-                    v[b * R + 2 * h + 1] = cmul(v[b * R + 2 * h + 1], make_float2(ww.z, ww.w));
-                });
-            } else {
-                sfor<R - 1>([&](auto rr) {
-                    constexpr int r = decltype(rr)::value + 1;
-                    v[b * R + r] = cmul(v[b * R + r], w[r]);
-                });
+        if (FULL || j < NBF) {
+            if constexpr (NS > 1) {
+                const int k = j % NS;
+                const float2* w = tw + tw_off + k * R;
+                if constexpr (R % 2 == 0) {
+                    sfor<R / 2>([&](auto hh) {
+                        constexpr int h = decltype(hh)::value;
+                        const float4 ww = reinterpret_cast<const float4*>(w)[h];
+                        if constexpr (h > 0) v[b * R + 2 * h] = cmul(v[b * R + 2 * h], make_float2(ww.x, ww.y));
+                        v[b * R + 2 * h + 1] = cmul(v[b * R + 2 * h + 1], make_float2(ww.z, ww.w));
+                    });
+                } else {
+                    sfor<R - 1>([&](auto rr) {
+                        constexpr int r = decltype(rr)::value + 1;
+                        v[b * R + r] = cmul(v[b * R + r], w[r]);
+                    });
+                }
             }
+            DFT<R>::run(&v[b * R]);
         }
-        DFT<R>::run(&v[b * R]);
     });
     // ---- store
     if (LAST && last_global) {
@@ -141,178 +164,186 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
                 });
             }
         });
-        __syncthreads();
+        group_sync(bar_id, S::NTHR);
     }
 }
 
-template <class S>
-__device__ __forceinline__ void codelet_passes(const PipeCtx& c, float2* W, float2 (&v)[S::E], const float2* tw,
-                                               const RowArgs& A, bool from_stage, bool last_global)
-{
-    sfor<S::NP>([&](auto pp) {
-        constexpr int P = decltype(pp)::value;
-        codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, from_stage, last_global);
-    });
-}
-
+// Shared-memory layout (byte offsets from the dynamic shared base):
+//   [0, smem_post)                  CTA header (unused 128 B) + pass tables at smem_tw
+//   [smem_post, smem_stage)         post-process twiddles
+//   [smem_stage + g*group_bytes)    group g: 64 B barriers/flags, NST slots of
+//                                   stage_bytes, then the work buffer (lpad float2)
 template <class S>
 __global__ void __launch_bounds__(512) codelet_kernel(const __grid_constant__ RowArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);
-    volatile int* flags = reinterpret_cast<int*>(smraw + 64);  // [0] abort, [1+s] manual copy of stage s
     float2* stw = reinterpret_cast<float2*>(smraw + A.smem_tw);
     float2* spost = reinterpret_cast<float2*>(smraw + A.smem_post);
-    unsigned char* stages = smraw + A.smem_stage;
-    float2* work = reinterpret_cast<float2*>(smraw + A.smem_work);
-
     constexpr int L = S::L;
-    const int tl = threadIdx.x / S::NTHR;
-    const int tid = threadIdx.x - tl * S::NTHR;
+    const int g = threadIdx.x / S::NTHR;
+    const int tid = threadIdx.x - g * S::NTHR;
+    const int NG = A.ngroups;
     const int NST = A.nstage;
-    const int64_t ntiles = (A.ntf + A.tfpc - 1) / A.tfpc;
+    const int TPS = A.tfpc;  // transforms per slot
+    const int bar_id = 1 + g;
+    const bool leader = tid == 0;
+    const int64_t group_bytes = (int64_t)A.group_bytes;
+    unsigned char* gbase = smraw + A.smem_stage + (int64_t)g * group_bytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(gbase);
+    volatile int* flags = reinterpret_cast<int*>(gbase + 32);  // [0] abort, [1+s] manual copy
+    unsigned char* slots = gbase + 64;
+    float2* W = reinterpret_cast<float2*>(slots + (int64_t)NST * A.stage_bytes);
+
     const int64_t row_bytes = A.in_dist * A.in_esize;
+    const int64_t nslots = (A.ntf + TPS - 1) / TPS;
+    const int64_t gstride = (int64_t)gridDim.x * NG;
+    const int64_t gfirst = (int64_t)blockIdx.x * NG + g;
     const float2* gtw = reinterpret_cast<const float2*>(A.tw);
     const float2* gpost = reinterpret_cast<const float2*>(A.post_tw);
 
     for (int i = threadIdx.x; i < A.tw_cnt; i += blockDim.x) stw[i] = ldg2(gtw + A.tw_lo + i);
     for (int i = threadIdx.x; i < A.post_cnt; i += blockDim.x) spost[i] = ldg2(gpost + i);
-    if (threadIdx.x == 0) {
+    if (leader) {
         for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
         flags[0] = 0;
         fence_mbar_init();
     }
-    __syncthreads();
+    __syncthreads();  // the only CTA-wide barrier
 
-    auto issue = [&](int s, int64_t tile) {
-        const int64_t t0 = tile * A.tfpc;
-        const int64_t rows = min((int64_t)A.tfpc, A.ntf - t0);
+    auto issue = [&](int s, int64_t slot) {  // group leader only
+        const int64_t t0 = slot * TPS;
+        const int64_t rows = min((int64_t)TPS, A.ntf - t0);
         const unsigned char* src = reinterpret_cast<const unsigned char*>(A.in) + t0 * row_bytes;
         const int64_t bytes = rows * row_bytes;
         if (((reinterpret_cast<uintptr_t>(src) | (uintptr_t)bytes) & 15) == 0) {
             flags[1 + s] = 0;
             mbar_expect_tx(&bars[s], (uint32_t)bytes);
-            bulk_copy_g2s(stages + (int64_t)s * A.stage_bytes, src, (uint32_t)bytes, &bars[s]);
+            bulk_copy_g2s(slots + (int64_t)s * A.stage_bytes, src, (uint32_t)bytes, &bars[s]);
         } else {
             flags[1 + s] = 1;
         }
     };
     uint32_t phase = 0;
-    if (threadIdx.x == 0) {
+    if (leader) {
         for (int s = 0; s < NST; ++s) {
-            const int64_t tile = blockIdx.x + (int64_t)s * gridDim.x;
-            if (tile < ntiles) issue(s, tile);
+            const int64_t slot = gfirst + (int64_t)s * gstride;
+            if (slot < nslots) issue(s, slot);
         }
     }
-    // pass tables: shared window (the planner guarantees it fits)
-    const float2* tw = stw;
-    const float2* post = A.post_cnt > 0 ? spost : gpost;
+    const float2* tw = stw - A.tw_lo;
+    const float2* post = spost;
     const bool staged = A.staged != 0;
     const bool last_global = !(A.io_mode == IO_R2C_EVEN || (A.io_mode == IO_C2C && staged));
-    float2* W = work + tl * A.lpad;
     float2 v[S::E];
 
     for (int64_t it = 0;; ++it) {
-        const int64_t tile = blockIdx.x + it * gridDim.x;
-        if (tile >= ntiles) break;
+        const int64_t slot = gfirst + it * gstride;
+        if (slot >= nslots) break;
         const int s = (int)(it % NST);
-        if (threadIdx.x == 0 && !flags[1 + s]) {
+        if (leader && !flags[1 + s]) {
             if (!mbar_wait_bounded(&bars[s], (phase >> s) & 1u)) flags[0] = 1;
             phase ^= 1u << s;
         }
-        __syncthreads();
+        group_sync(bar_id, S::NTHR);
         if (flags[0]) {
-            if (threadIdx.x == 0) {
+            if (leader) {
                 atomicOr(A.err, 1);
                 for (int k = 1; k < NST; ++k) {
                     const int s2 = (s + k) % NST;
-                    const int64_t t2 = blockIdx.x + (it + k) * gridDim.x;
-                    if (t2 < ntiles && !flags[1 + s2]) mbar_wait_bounded(&bars[s2], (phase >> s2) & 1u);
+                    const int64_t sl2 = gfirst + (it + k) * gstride;
+                    if (sl2 < nslots && !flags[1 + s2]) mbar_wait_bounded(&bars[s2], (phase >> s2) & 1u);
                 }
             }
-            return;
+            break;
         }
-        unsigned char* stg = stages + (int64_t)s * A.stage_bytes;
-        const int64_t t0 = tile * A.tfpc;
-        const int rows = (int)min((int64_t)A.tfpc, A.ntf - t0);
+        unsigned char* stg = slots + (int64_t)s * A.stage_bytes;
+        const int64_t t0 = slot * TPS;
+        const int rows = (int)min((int64_t)TPS, A.ntf - t0);
         if (flags[1 + s]) {
-            coop_copy(stg, reinterpret_cast<const unsigned char*>(A.in) + t0 * row_bytes, rows * row_bytes);
-            __syncthreads();
+            const unsigned char* src = reinterpret_cast<const unsigned char*>(A.in) + t0 * row_bytes;
+            const int64_t bytes = rows * row_bytes;
+            for (int64_t i = tid; i < bytes / 4; i += S::NTHR)
+                reinterpret_cast<float*>(stg)[i] = __ldg(reinterpret_cast<const float*>(src) + i);
+            group_sync(bar_id, S::NTHR);
         }
-        PipeCtx c;
-        c.L = L;
-        c.nthr = S::NTHR;
-        c.tid = tid;
-        c.ok_sm = true;
-        c.ok_io = tl < rows;
-        c.pshift = S::PSHIFT;
-        c.tw = tw;
-        c.sA = W;
-        c.sB = W;
-        c.st2 = reinterpret_cast<const float2*>(stg + (int64_t)tl * row_bytes);
-        c.st1 = reinterpret_cast<const float*>(c.st2);
-        c.mode = A.io_mode;
-        c.conj_in = A.conj_in;
-        c.conj_out = A.conj_out;
-        c.weight = A.weight;
-        c.nreal = A.nreal;
-        c.scale = A.scale;
-        const int64_t tt = c.ok_io ? t0 + tl : 0;
-        c.out2 = reinterpret_cast<float2*>(A.out) + tt * A.out_dist;
-        c.out1 = reinterpret_cast<float*>(A.out) + tt * A.out_dist;
+        for (int q = 0; q < rows; ++q) {
+            PipeCtx c;
+            c.L = L;
+            c.nthr = S::NTHR;
+            c.tid = tid;
+            c.ok_sm = true;
+            c.ok_io = true;
+            c.pshift = S::PSHIFT;
+            c.tw = tw;
+            c.sA = W;
+            c.sB = W;
+            c.st2 = reinterpret_cast<const float2*>(stg + (int64_t)q * row_bytes);
+            c.st1 = reinterpret_cast<const float*>(c.st2);
+            c.mode = A.io_mode;
+            c.conj_in = A.conj_in;
+            c.conj_out = A.conj_out;
+            c.weight = A.weight;
+            c.nreal = A.nreal;
+            c.scale = A.scale;
+            const int64_t tt = t0 + q;
+            c.out2 = reinterpret_cast<float2*>(A.out) + tt * A.out_dist;
+            c.out1 = reinterpret_cast<float*>(A.out) + tt * A.out_dist;
 
-        bool from_stage = true;
-        if (A.io_mode == IO_C2R_EVEN) {
-            // pre-process pairs (k, L-k) from the stage into W (see row_pipe.cuh)
-            const bool half = A.weight == WEIGHT_LOAD_HALF;
-            for (int k = tid; k <= (L >> 1); k += S::NTHR) {
-                if (k == 0) {
-                    const float x0 = c.st2[0].x, xl = c.st2[L].x;
-                    W[0] = make_float2(x0 + xl, -(x0 - xl));
-                } else {
-                    float2 a = c.st2[k], b = c.st2[L - k];
-                    if (half) {
-                        a = cscale(a, 0.5f);
-                        b = cscale(b, 0.5f);
+            bool from_slot = true;
+            if (A.io_mode == IO_C2R_EVEN) {
+                // pre-process pairs (k, L-k) from the slot into W:
+                //   Z'[k] = E + i*O,  E = X[k] + conj(X[L-k]),
+                //   O = (X[k] - conj(X[L-k])) * conj(W_N^k), stored conjugated.
+                const bool half = A.weight == WEIGHT_LOAD_HALF;
+                for (int k = tid; k <= (L >> 1); k += S::NTHR) {
+                    if (k == 0) {
+                        const float x0 = c.st2[0].x, xl = c.st2[L].x;  // Im of DC/Nyquist ignored
+                        W[0] = make_float2(x0 + xl, -(x0 - xl));
+                    } else {
+                        float2 a = c.st2[k], b = c.st2[L - k];
+                        if (half) {
+                            a = cscale(a, 0.5f);
+                            b = cscale(b, 0.5f);
+                        }
+                        const float2 w = post[k];
+                        const float2 bc = cconj(b);
+                        const float2 e = cadd(a, bc);
+                        const float2 o = cmulc(csub(a, bc), w);
+                        W[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
+                        if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
                     }
-                    const float2 w = post[k];
-                    const float2 bc = cconj(b);
-                    const float2 e = cadd(a, bc);
-                    const float2 o = cmulc(csub(a, bc), w);
-                    W[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
-                    if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
+                }
+                group_sync(bar_id, S::NTHR);
+                from_slot = false;
+            }
+            codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, from_slot, last_global, bar_id);
+            // after the slot's last transform has been read, refill the slot
+            if (q == rows - 1 && leader) {
+                const int64_t nsl = gfirst + (it + NST) * gstride;
+                if (nsl < nslots) {
+                    fence_proxy_async_smem();
+                    issue(s, nsl);
                 }
             }
-            __syncthreads();
-            from_stage = false;
-        }
-        // the first pass (or the pre-process) consumes the stage: it is
-        // refilled once pass 0 has loaded its registers
-        if (from_stage) {
-            codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, true, last_global);
-        }
-        if (threadIdx.x == 0) {
-            const int64_t nt = blockIdx.x + (it + NST) * gridDim.x;
-            if (nt < ntiles) {
-                fence_proxy_async_smem();
-                issue(s, nt);
-            }
-        }
-        if (!from_stage) {
-            codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, false, last_global);
-        }
-        sfor<S::NP - 1>([&](auto pp) {
-            constexpr int P = decltype(pp)::value + 1;
-            codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, false, last_global);
-        });
+            sfor<S::NP - 1>([&](auto pp) {
+                constexpr int P = decltype(pp)::value + 1;
+                codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, false, last_global, bar_id);
+            });
 
-        if (A.io_mode == IO_C2C && staged) {
-            rows_to_global(work, A.lpad, S::PSHIFT, reinterpret_cast<float2*>(A.out) + t0 * A.out_dist, A.out_dist,
-                           rows, L, A.conj_out != 0, A.scale);
-        } else if (A.io_mode == IO_R2C_EVEN) {
-            const float sc = A.scale;
-            const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
-            if (c.ok_io) {
+            if (A.io_mode == IO_C2C && staged) {
+                for (int i = tid; i < L; i += S::NTHR) {
+                    float2 x = W[cpad<S>(i)];
+                    if (A.conj_out) x = cconj(x);
+                    c.out2[i] = cscale(x, A.scale);
+                }
+                group_sync(bar_id, S::NTHR);
+            } else if (A.io_mode == IO_R2C_EVEN) {
+                // post-process pairs:
+                //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
+                //   X[k] = E + W^k O, X[L-k] = conj(E - W^k O),
+                //   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0 (zero imaginary parts)
+                const float sc = A.scale;
+                const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
                 for (int k = tid; k <= (L >> 1); k += S::NTHR) {
                     if (k == 0) {
                         const float2 z0 = W[0];
@@ -327,9 +358,9 @@ __global__ void __launch_bounds__(512) codelet_kernel(const __grid_constant__ Ro
                         if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
                     }
                 }
+                group_sync(bar_id, S::NTHR);
             }
         }
-        __syncthreads();
     }
 }
 

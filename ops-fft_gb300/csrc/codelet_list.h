@@ -4,12 +4,12 @@
 // translation unit (codelet_<id>.cu) so the build runs in parallel.
 #pragma once
 #define GFFT_CODELETS(X)                 \
-    X(0, 1500, 150, 15, 10, 10)          \
-    X(1, 512, 64, 8, 8, 8)               \
+    X(0, 1500, 160, 15, 10, 10)          \
+    X(1, 512, 32, 8, 8, 8)               \
     X(2, 4096, 256, 16, 16, 16)          \
     X(3, 2048, 128, 16, 16, 8)           \
     X(4, 1024, 64, 16, 16, 4)            \
-    X(5, 256, 16, 16, 16)                \
-    X(6, 128, 16, 16, 8)                 \
+    X(5, 256, 32, 16, 16)                \
+    X(6, 128, 32, 8, 16)                 \
     X(7, 8192, 512, 16, 16, 16, 2)
 #define GFFT_NUM_CODELETS 8

@@ -78,6 +78,8 @@ struct RowArgs {
     int32_t smem_tw, smem_post, smem_stage, smem_work, smem_bytes;  // byte offsets / total
     int32_t grid;      // persistent CTAs (0: SMs x occupancy)
     int32_t codelet;   // compile-time specialised kernel id, -1 for the generic kernel
+    int32_t ngroups;   // codelets: transform groups per CTA
+    int32_t group_bytes;  // codelets: shared bytes per group (barriers, slots, work buffer)
 };
 
 // Strided ("column") transforms, optionally one outer Stockham pass of a

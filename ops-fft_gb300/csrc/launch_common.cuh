@@ -82,8 +82,9 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
 {
     static unsigned long long attr_mask = 0;
     static thread_local int last_threads = -1, last_smem = -1, last_occ = 1;
-    const int threads = S::NTHR * a->tfpc;
-    if (a->ip.L != S::L || threads <= 0 || threads > 512 || a->ntf <= 0) return (int)cudaErrorInvalidValue;
+    const int threads = S::NTHR * a->ngroups;
+    if (a->ip.L != S::L || a->ngroups < 1 || a->ngroups > 15 || threads > 512 || a->ntf <= 0)
+        return (int)cudaErrorInvalidValue;
     if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
         return (int)cudaErrorInvalidValue;
     cudaError_t e = ensure_smem_attr(codelet_kernel<S>, attr_mask, (size_t)a->smem_bytes);
@@ -96,11 +97,12 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
         last_smem = a->smem_bytes;
         last_occ = occ < 1 ? 1 : occ;
     }
-    const int64_t ntiles = (a->ntf + a->tfpc - 1) / a->tfpc;
+    const int64_t nslots = (a->ntf + a->tfpc - 1) / a->tfpc;
+    const int64_t ctas_needed = (nslots + a->ngroups - 1) / a->ngroups;
     int64_t grid = (int64_t)sm_count() * last_occ;
     if (a->grid > 0) grid = a->grid;
     if (grid < 1) grid = 1;
-    if (grid > ntiles) grid = ntiles;
+    if (grid > ctas_needed) grid = ctas_needed;
     codelet_kernel<S><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
     return (int)cudaGetLastError();
 }

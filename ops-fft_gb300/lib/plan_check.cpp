@@ -73,8 +73,9 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const RowArgs& a = s.row;
     if (!check_inner(a.ip, tw_count, why)) return false;
     const int L = a.ip.L;
-    const int maxthr = (a.ip.rmax == 16 || a.codelet >= 0) ? 512 : 256;
-    if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1) return fail(why, "row threads");
+    const int maxthr = a.ip.rmax == 16 ? 512 : 256;
+    if (a.codelet < 0 && (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1)) return fail(why, "row threads");
+    if (a.tfpc < 1) return fail(why, "row tile");
     if (a.nstage < 1 || a.nstage > 4) return fail(why, "row stages");
     if (a.codelet >= 0) {
         int cn = 0, cr[kMaxPass], cnr = 0;
@@ -94,7 +95,15 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     if (maxidx + (maxidx >> a.pshift) >= a.lpad) return fail(why, "row lpad too small");
     const int64_t row_bytes = a.in_dist * a.in_esize;
     if ((int64_t)a.tfpc * row_bytes > a.stage_bytes || a.stage_bytes % 16) return fail(why, "row stage too small");
-    if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
+    if (a.codelet >= 0) {
+        const int64_t slots_end = 64 + (int64_t)a.nstage * a.stage_bytes;
+        if (a.ngroups < 1 || a.ngroups > 15 || a.ngroups * a.ip.nthr > 512) return fail(why, "codelet groups");
+        if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
+            a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 128 || a.group_bytes % 128 ||
+            a.stage_bytes % 16 || slots_end + (int64_t)a.lpad * 8 > a.group_bytes ||
+            a.smem_bytes < a.smem_stage + (int64_t)a.ngroups * a.group_bytes || a.smem_bytes > kMaxSmemBytes)
+            return fail(why, "codelet shared-memory layout");
+    } else if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
         a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 16 ||
         a.smem_work < a.smem_stage + (int64_t)a.nstage * a.stage_bytes ||
         a.smem_bytes < a.smem_work + (int64_t)a.tfpc * a.nbuf * a.lpad * 8 || a.smem_bytes > kMaxSmemBytes)

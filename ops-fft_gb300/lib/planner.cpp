@@ -172,6 +172,110 @@ int col_max_length() { return 2048; }
 
 namespace {
 
+// Codelet row step (see csrc/codelet.cuh for the execution model and the
+// shared-memory layout).  Returns false when no codelet applies.
+bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io_mode, int nreal, int weight,
+                       TwiddleBuilder& tb, Step& st)
+{
+    if (!codelets_enabled()) return false;
+    int cn = 0, cr[kMaxPass], cnr = 0;
+    const int id = gfft_codelet_lookup(L, &cn, cr, &cnr);
+    if (id < 0) return false;
+    const std::vector<int> rad(cr, cr + cnr);
+    const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
+    const bool staged = false;
+    const int pshift = (rad[0] % 2 == 0) ? 4 : 30;
+    const int maxidx = even_mode ? L : L - 1;
+    int lpad = maxidx + (maxidx >> pshift) + 2;
+    lpad += lpad & 1;
+    const int esize = io_mode == IO_R2C_ODD ? 4 : 8;
+    const int64_t row_bytes = in_dist * esize;
+    TwiddleBuilder trial = tb;  // do not register tables unless the codelet is used
+    st = Step{};
+    st.kind = Step::ROW;
+    RowArgs& a = st.row;
+    if (!build_inner(L, rad, cn, trial, a.ip)) return false;
+    int64_t lo = -1, hi = -1;
+    for (int p = 0; p < a.ip.npass; ++p) {
+        const PassDesc& d = a.ip.pass[p];
+        if (d.ns <= 1) continue;
+        lo = lo < 0 ? d.tw_off : std::min<int64_t>(lo, d.tw_off);
+        hi = std::max<int64_t>(hi, d.tw_off + (int64_t)d.ns * d.radix);
+    }
+    const int64_t tw_cnt = lo < 0 ? 0 : hi - lo;
+    const int64_t post_cnt = even_mode ? L / 2 + 1 : 0;
+    int64_t post_off = -1;
+    if (even_mode) post_off = trial.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
+    auto align = [](int64_t x, int64_t a) { return (x + a - 1) / a * a; };
+    const int64_t hdr = 128;
+    const int64_t tw_bytes = align(tw_cnt * 8, 16);
+    const int64_t post_bytes = align(post_cnt * 8, 16);
+    int tps = 1;
+    while ((row_bytes * tps) % 16 != 0 && tps < 16) tps *= 2;
+    const int64_t stage_bytes = align(tps * row_bytes, 16);
+    const int64_t work_bytes = align((int64_t)lpad * 8, 16);
+    const int64_t cta_fixed = align(hdr + tw_bytes + post_bytes, 128);
+    const int64_t nslots = (ntf + tps - 1) / tps;
+    double best = -1;
+    int best_ng = 0, best_ns = 0;
+    int64_t best_gb = 0;
+    for (int nst = 2; nst <= 3; ++nst) {
+        const int64_t gb = align(64 + nst * stage_bytes + work_bytes, 128);
+        for (int ng = 1; ng <= 15 && ng * cn <= 512; ++ng) {
+            const int64_t smem = cta_fixed + ng * gb;
+            if (smem > kMaxSmemBytes) break;
+            const int64_t warps = (int64_t)ng * cn / 32;
+            const int64_t ctas = std::min<int64_t>({(228 * 1024) / (smem + 1024), 64 / warps, 32});
+            if (ctas < 1) continue;
+            int64_t groups_sm = ctas * ng;
+            // a small batch cannot keep every group busy
+            groups_sm = std::min<int64_t>(groups_sm, std::max<int64_t>(1, (nslots + 151) / 152));
+            const double occ = (double)std::min<int64_t>(groups_sm * cn, 1536) / 1536.0;
+            const double infl =
+                (double)std::min<int64_t>(groups_sm * (nst - 1) * tps * row_bytes, 64 * 1024) / (64 * 1024.0);
+            const double score = occ + infl - 0.02 * nst;
+            if (score > best + 1e-9) {
+                best = score;
+                best_ng = ng;
+                best_ns = nst;
+                best_gb = gb;
+            }
+        }
+    }
+    if (best < 0) return false;
+    tb = trial;
+    st.post_off = post_off;
+    a.ntf = ntf;
+    a.in_dist = in_dist;
+    a.out_dist = out_dist;
+    a.tfpc = tps;
+    a.lpad = lpad;
+    a.nbuf = 1;
+    a.io_mode = io_mode;
+    a.weight = weight;
+    a.nreal = nreal;
+    a.staged = staged ? 1 : 0;
+    a.scale = 1.f;
+    a.conj_out = io_mode == IO_C2R_EVEN ? 1 : 0;
+    a.nstage = best_ns;
+    a.pshift = pshift;
+    a.in_esize = esize;
+    a.tw_lo = (int32_t)(lo < 0 ? 0 : lo);
+    a.tw_cnt = (int32_t)tw_cnt;
+    a.post_cnt = (int32_t)post_cnt;
+    a.stage_bytes = (int32_t)stage_bytes;
+    a.smem_tw = (int32_t)hdr;
+    a.smem_post = (int32_t)(hdr + tw_bytes);
+    a.smem_stage = (int32_t)cta_fixed;
+    a.smem_work = 0;
+    a.group_bytes = (int32_t)best_gb;
+    a.ngroups = best_ng;
+    a.smem_bytes = (int32_t)(cta_fixed + best_ng * best_gb);
+    a.codelet = id;
+    st.tw_off = 0;
+    return true;
+}
+
 // One on-chip transform per contiguous batch item (persistent row kernel,
 // see csrc/row_pipe.cuh for the shared-memory layout).
 bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io_mode, int nreal, int weight,
@@ -182,24 +286,13 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     int rmax = *std::max_element(rad.begin(), rad.end()) > 16 ? 47 : 16;
     int maxthr = max_threads_for(rmax);
     int nthr = pick_nthr(L, rad, maxthr);
-    // compile-time specialised kernel for this length, when one is built
     int codelet = -1;
-    if (codelets_enabled()) {
-        int cn = 0, cr[kMaxPass], cnr = 0;
-        const int id = gfft_codelet_lookup(L, &cn, cr, &cnr);
-        if (id >= 0) {
-            codelet = id;
-            nthr = cn;
-            rad.assign(cr, cr + cnr);
-            rmax = 16;
-            maxthr = 512;
-        }
-    }
+    if (make_codelet_step(L, ntf, in_dist, out_dist, io_mode, nreal, weight, tb, st)) return true;
     const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
     const bool staged = nthr < 32 && (io_mode == IO_C2C || io_mode == IO_R2C_EVEN);
     const int start = io_mode == IO_C2R_EVEN ? 1 : 0;
     const bool last_global = !(io_mode == IO_R2C_EVEN || (io_mode == IO_C2C && staged));
-    const int nbuf = codelet >= 0 ? 1 : std::max(1, row_nbuf((int)rad.size(), start, last_global));
+    const int nbuf = std::max(1, row_nbuf((int)rad.size(), start, last_global));
     const int pshift = (rad[0] % 2 == 0) ? 4 : 30;
     const int maxidx = even_mode ? L : L - 1;
     int lpad = maxidx + (maxidx >> pshift) + 2;
@@ -222,7 +315,7 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     }
     const int64_t tw_cnt = lo < 0 ? 0 : hi - lo;
     const bool tw_in_smem = tw_cnt * 8 <= 72 * 1024;
-    if (codelet >= 0 && !tw_in_smem) return false;  // codelets read twiddles from shared memory only
+
     const int64_t post_cnt = even_mode ? L / 2 + 1 : 0;
     if (even_mode) st.post_off = tb.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
 
@@ -287,6 +380,8 @@ bool make_row_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io
     a.smem_work = (int32_t)(a.smem_stage + (int64_t)best_ns * a.stage_bytes);
     a.smem_bytes = (int32_t)(a.smem_work + (int64_t)best_tf * nbuf * lpad * 8);
     a.codelet = codelet;
+    a.ngroups = 0;
+    a.group_bytes = 0;
     (void)best_smem;
     st.tw_off = 0;
     return a.smem_bytes <= kMaxSmemBytes;
