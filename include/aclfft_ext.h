@@ -53,6 +53,10 @@ typedef struct aclfftPlanInfo_t {
     int transforms_per_cta;
     long long twiddle_entries; /* complex entries generated on the GPU */
     size_t workspace_bytes;    /* device workspace owned by the plan */
+    int kernel;                /* first step: -1 generic row/column kernel, >= 0 specialised codelet id */
+    int groups_per_cta;        /* codelets: independent transform groups per CTA */
+    int stages;                /* input prefetch stages */
+    int smem_bytes;            /* dynamic shared memory per CTA */
 } aclfftPlanInfo;
 
 ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info);

@@ -64,6 +64,10 @@ class PlanInfo(ctypes.Structure):
         ("transforms_per_cta", ctypes.c_int),
         ("twiddle_entries", ctypes.c_longlong),
         ("workspace_bytes", ctypes.c_size_t),
+        ("kernel", ctypes.c_int),
+        ("groups_per_cta", ctypes.c_int),
+        ("stages", ctypes.c_int),
+        ("smem_bytes", ctypes.c_int),
     ]
 
 

@@ -32,8 +32,10 @@
 
 namespace gfft {
 
-template <int L_, int NTHR_, int... Rs>
+template <int MAXT_, int MINB_, int L_, int NTHR_, int... Rs>
 struct CSpec {
+    static constexpr int MAXT = MAXT_;  // launch bound: threads per CTA
+    static constexpr int MINB = MINB_;  // CTAs per SM the register budget must allow
     static constexpr int L = L_;
     static constexpr int NTHR = NTHR_;
     static constexpr int NP = sizeof...(Rs);
@@ -88,18 +90,29 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
     constexpr bool FULL = (NBF % S::NTHR) == 0;
     constexpr bool LAST = P == S::NP - 1;
     const int tid = c.tid;
-    // ---- load
+    // ---- load (the io mode is uniform: branch once, outside the unrolled loops)
     if (P == 0 && from_slot) {
-        sfor<NB>([&](auto bb) {
-            constexpr int b = decltype(bb)::value;
-            const int j = tid + b * S::NTHR;
-            if (FULL || j < NBF) {
-                sfor<R>([&](auto rr) {
-                    constexpr int r = decltype(rr)::value;
-                    v[b * R + r] = c.gload(j + r * NBF);
-                });
-            }
-        });
+        auto load_all = [&](auto getter) {
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                const int j = tid + b * S::NTHR;
+                if (FULL || j < NBF) {
+                    sfor<R>([&](auto rr) {
+                        constexpr int r = decltype(rr)::value;
+                        v[b * R + r] = getter(j + r * NBF);
+                    });
+                }
+            });
+        };
+        if (c.mode == IO_R2C_ODD) {
+            load_all([&](int i) { return make_float2(c.st1[i], 0.f); });
+        } else if (c.mode == IO_C2R_ODD) {
+            load_all([&](int i) { return c.gload(i); });
+        } else if (c.conj_in) {
+            load_all([&](int i) { return cconj(c.st2[i]); });
+        } else {
+            load_all([&](int i) { return c.st2[i]; });
+        }
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -140,16 +153,32 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
     });
     // ---- store
     if (LAST && last_global) {
-        sfor<NB>([&](auto bb) {
-            constexpr int b = decltype(bb)::value;
-            const int j = tid + b * S::NTHR;
-            if ((FULL || j < NBF) && c.ok_io) {
-                sfor<R>([&](auto rr) {
-                    constexpr int r = decltype(rr)::value;
-                    c.gstore(j + r * NS, v[b * R + r]);
-                });
+        auto store_all = [&](auto putter) {
+            sfor<NB>([&](auto bb) {
+                constexpr int b = decltype(bb)::value;
+                const int j = tid + b * S::NTHR;
+                if (FULL || j < NBF) {
+                    sfor<R>([&](auto rr) {
+                        constexpr int r = decltype(rr)::value;
+                        putter(j + r * NS, v[b * R + r]);
+                    });
+                }
+            });
+        };
+        if (c.ok_io) {
+            const float sc = c.scale;
+            if (c.mode == IO_C2C || c.mode == IO_C2R_EVEN) {
+                if (c.conj_out) {
+                    store_all([&](int i, float2 x) { c.out2[i] = make_float2(x.x * sc, -x.y * sc); });
+                } else if (sc == 1.f) {
+                    store_all([&](int i, float2 x) { c.out2[i] = x; });
+                } else {
+                    store_all([&](int i, float2 x) { c.out2[i] = cscale(x, sc); });
+                }
+            } else {
+                store_all([&](int i, float2 x) { c.gstore(i, x); });
             }
-        });
+        }
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -174,7 +203,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
 //   [smem_stage + g*group_bytes)    group g: 64 B barriers/flags, NST slots of
 //                                   stage_bytes, then the work buffer (lpad float2)
 template <class S>
-__global__ void __launch_bounds__(512) codelet_kernel(const __grid_constant__ RowArgs A)
+__global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_constant__ RowArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
     float2* stw = reinterpret_cast<float2*>(smraw + A.smem_tw);

@@ -4,19 +4,19 @@
 #include "launch_common.cuh"
 
 namespace gfft {
-#define GFFT_INST(ID, L, NT, ...)                                                        \
+#define GFFT_INST(ID, MT, MB, L, NT, ...)                                                        \
     int launch_codelet_##ID(const RowArgs* a, cudaStream_t st)                           \
     {                                                                                    \
-        return launch_codelet_t<CSpec<L, NT, __VA_ARGS__>>(a, st);                       \
+        return launch_codelet_t<CSpec<MT, MB, L, NT, __VA_ARGS__>>(a, st);                       \
     }
-#define GFFT_PICK(ID, L, NT, ...) GFFT_PICK_##ID(ID, L, NT, __VA_ARGS__)
-#define GFFT_PICK_1(ID, L, NT, ...) GFFT_INST(ID, L, NT, __VA_ARGS__)
-#define GFFT_PICK_0(ID, L, NT, ...)
-#define GFFT_PICK_2(ID, L, NT, ...)
-#define GFFT_PICK_3(ID, L, NT, ...)
-#define GFFT_PICK_4(ID, L, NT, ...)
-#define GFFT_PICK_5(ID, L, NT, ...)
-#define GFFT_PICK_6(ID, L, NT, ...)
-#define GFFT_PICK_7(ID, L, NT, ...)
+#define GFFT_PICK(ID, MT, MB, L, NT, ...) GFFT_PICK_##ID(ID, MT, MB, L, NT, __VA_ARGS__)
+#define GFFT_PICK_1(ID, MT, MB, L, NT, ...) GFFT_INST(ID, MT, MB, L, NT, __VA_ARGS__)
+#define GFFT_PICK_0(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_2(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_3(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_4(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_5(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_6(ID, MT, MB, L, NT, ...)
+#define GFFT_PICK_7(ID, MT, MB, L, NT, ...)
 GFFT_CODELETS(GFFT_PICK)
 }  // namespace gfft

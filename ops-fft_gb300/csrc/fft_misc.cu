@@ -141,10 +141,17 @@ extern "C" int gfft_gen_twiddles(void* table, const TwSeg* segs, int nseg, void*
 
 extern "C" int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix)
 {
-#define GFFT_LOOKUP(ID, LL, NT, ...)                           \
+    int maxt = 0;
+    return gfft_codelet_lookup2(L, nthr, radices, nradix, &maxt);
+}
+
+extern "C" int gfft_codelet_lookup2(int L, int* nthr, int* radices, int* nradix, int* maxt)
+{
+#define GFFT_LOOKUP(ID, MT, MB, LL, NT, ...)                           \
     if (L == LL) {                                             \
         const int r[] = {__VA_ARGS__};                         \
         *nthr = NT;                                            \
+        *maxt = MT;                                            \
         *nradix = (int)(sizeof(r) / sizeof(r[0]));             \
         for (int i = 0; i < *nradix; ++i) radices[i] = r[i];   \
         return ID;                                             \

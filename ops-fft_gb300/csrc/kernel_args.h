@@ -151,4 +151,5 @@ int gfft_kernel_max_threads(int rmax);
 // Compile-time specialised row kernel for length L: returns its id (or -1)
 // and fills its thread count per transform and radix sequence.
 int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix);
+int gfft_codelet_lookup2(int L, int* nthr, int* radices, int* nradix, int* max_threads_per_cta);
 }

@@ -83,7 +83,7 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
     static unsigned long long attr_mask = 0;
     static thread_local int last_threads = -1, last_smem = -1, last_occ = 1;
     const int threads = S::NTHR * a->ngroups;
-    if (a->ip.L != S::L || a->ngroups < 1 || a->ngroups > 15 || threads > 512 || a->ntf <= 0)
+    if (a->ip.L != S::L || a->ngroups < 1 || a->ngroups > 15 || threads > S::MAXT || a->ntf <= 0)
         return (int)cudaErrorInvalidValue;
     if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
         return (int)cudaErrorInvalidValue;

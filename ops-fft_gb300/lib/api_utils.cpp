@@ -131,9 +131,14 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
     for (const gfft::Step& s : sl.steps) {
         const gfft::InnerPlan* ip = nullptr;
         int tf = 0;
+        info->kernel = -1;
         if (s.kind == gfft::Step::ROW) {
             ip = &s.row.ip;
             tf = s.row.tfpc;
+            info->kernel = s.row.codelet;
+            info->groups_per_cta = s.row.ngroups;
+            info->stages = s.row.nstage;
+            info->smem_bytes = s.row.smem_bytes;
         } else if (s.kind == gfft::Step::COL) {
             ip = &s.col.ip;
             tf = s.col.tfpc;

@@ -178,8 +178,8 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
                        TwiddleBuilder& tb, Step& st)
 {
     if (!codelets_enabled()) return false;
-    int cn = 0, cr[kMaxPass], cnr = 0;
-    const int id = gfft_codelet_lookup(L, &cn, cr, &cnr);
+    int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
+    const int id = gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt);
     if (id < 0) return false;
     const std::vector<int> rad(cr, cr + cnr);
     const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
@@ -221,11 +221,14 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     int64_t best_gb = 0;
     for (int nst = 2; nst <= 3; ++nst) {
         const int64_t gb = align(64 + nst * stage_bytes + work_bytes, 128);
-        for (int ng = 1; ng <= 15 && ng * cn <= 512; ++ng) {
+        for (int ng = 1; ng <= 15 && ng * cn <= cmaxt; ++ng) {
             const int64_t smem = cta_fixed + ng * gb;
             if (smem > kMaxSmemBytes) break;
             const int64_t warps = (int64_t)ng * cn / 32;
-            const int64_t ctas = std::min<int64_t>({(228 * 1024) / (smem + 1024), 64 / warps, 32});
+            // registers: the launch bound caps each thread at 65536 / (MAXT * MINB)
+            const int64_t reg_cap = cmaxt <= 384 ? 80 : 128;
+            const int64_t ctas = std::min<int64_t>(
+                {(228 * 1024) / (smem + 1024), 64 / warps, 32, 65536 / (reg_cap * 32 * warps)});
             if (ctas < 1) continue;
             int64_t groups_sm = ctas * ng;
             // a small batch cannot keep every group busy
