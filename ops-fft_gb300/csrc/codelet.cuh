@@ -69,7 +69,11 @@ struct CSpec {
 template <class S>
 __device__ __forceinline__ int cpad(int i)
 {
-    return i + (i >> S::PSHIFT);
+    if constexpr (S::PSHIFT >= 30) {
+        return i;  // odd first radix: stride-R writes are already conflict free
+    } else {
+        return i + (i >> S::PSHIFT);
+    }
 }
 
 __device__ __forceinline__ void group_sync(int id, int nthreads)
@@ -113,6 +117,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
         } else {
             load_all([&](int i) { return c.st2[i]; });
         }
+        group_sync(bar_id, S::NTHR);  // the raw row and the padded work layout share the slot
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -198,10 +203,20 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
 }
 
 // Shared-memory layout (byte offsets from the dynamic shared base):
-//   [0, smem_post)                  CTA header (unused 128 B) + pass tables at smem_tw
-//   [smem_post, smem_stage)         post-process twiddles
-//   [smem_stage + g*group_bytes)    group g: 64 B barriers/flags, NST slots of
-//                                   stage_bytes, then the work buffer (lpad float2)
+//   [smem_tw, ...)                 pass tables (CTA-wide)
+//   [smem_post, ...)               post-process twiddles (CTA-wide)
+//   [smem_stage + g*group_bytes)   group g: 64 B barriers/flags, then NST
+//                                  slots of stage_bytes.  A slot holds one
+//                                  transform: its raw input row at offset
+//                                  src % 16, then (in place, from offset 16)
+//                                  the padded work layout.
+//
+// Slot fill: the row of transform t starts at src = in + t*row_bytes and is
+// placed at slot + (src % 16), so the 16-byte aligned superset
+// [src - src%16, ceil16(src + row_bytes)) is copied by one bulk copy.  The
+// superset only touches bytes of the neighbouring rows of the same buffer;
+// when it would reach outside the buffer (first/last row with unaligned
+// ends) the group copies the row with ordinary loads instead.
 template <class S>
 __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_constant__ RowArgs A)
 {
@@ -213,20 +228,18 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
     const int tid = threadIdx.x - g * S::NTHR;
     const int NG = A.ngroups;
     const int NST = A.nstage;
-    const int TPS = A.tfpc;  // transforms per slot
     const int bar_id = 1 + g;
     const bool leader = tid == 0;
-    const int64_t group_bytes = (int64_t)A.group_bytes;
-    unsigned char* gbase = smraw + A.smem_stage + (int64_t)g * group_bytes;
+    unsigned char* gbase = smraw + A.smem_stage + (int64_t)g * A.group_bytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(gbase);
     volatile int* flags = reinterpret_cast<int*>(gbase + 32);  // [0] abort, [1+s] manual copy
     unsigned char* slots = gbase + 64;
-    float2* W = reinterpret_cast<float2*>(slots + (int64_t)NST * A.stage_bytes);
 
     const int64_t row_bytes = A.in_dist * A.in_esize;
-    const int64_t nslots = (A.ntf + TPS - 1) / TPS;
     const int64_t gstride = (int64_t)gridDim.x * NG;
     const int64_t gfirst = (int64_t)blockIdx.x * NG + g;
+    const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(A.in);
+    const uintptr_t buf_hi = buf_lo + (uintptr_t)(A.ntf * row_bytes);
     const float2* gtw = reinterpret_cast<const float2*>(A.tw);
     const float2* gpost = reinterpret_cast<const float2*>(A.post_tw);
 
@@ -239,15 +252,15 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
     }
     __syncthreads();  // the only CTA-wide barrier
 
-    auto issue = [&](int s, int64_t slot) {  // group leader only
-        const int64_t t0 = slot * TPS;
-        const int64_t rows = min((int64_t)TPS, A.ntf - t0);
-        const unsigned char* src = reinterpret_cast<const unsigned char*>(A.in) + t0 * row_bytes;
-        const int64_t bytes = rows * row_bytes;
-        if (((reinterpret_cast<uintptr_t>(src) | (uintptr_t)bytes) & 15) == 0) {
+    auto issue = [&](int s, int64_t t) {  // group leader only
+        const uintptr_t src = buf_lo + (uintptr_t)(t * row_bytes);
+        const uintptr_t c0 = src & ~(uintptr_t)15;
+        const uintptr_t c1 = (src + (uintptr_t)row_bytes + 15) & ~(uintptr_t)15;
+        if (c0 >= buf_lo && c1 <= buf_hi) {
             flags[1 + s] = 0;
-            mbar_expect_tx(&bars[s], (uint32_t)bytes);
-            bulk_copy_g2s(slots + (int64_t)s * A.stage_bytes, src, (uint32_t)bytes, &bars[s]);
+            mbar_expect_tx(&bars[s], (uint32_t)(c1 - c0));
+            bulk_copy_g2s(slots + (int64_t)s * A.stage_bytes, reinterpret_cast<const void*>(c0),
+                          (uint32_t)(c1 - c0), &bars[s]);
         } else {
             flags[1 + s] = 1;
         }
@@ -255,19 +268,19 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
     uint32_t phase = 0;
     if (leader) {
         for (int s = 0; s < NST; ++s) {
-            const int64_t slot = gfirst + (int64_t)s * gstride;
-            if (slot < nslots) issue(s, slot);
+            const int64_t t = gfirst + (int64_t)s * gstride;
+            if (t < A.ntf) issue(s, t);
         }
     }
     const float2* tw = stw - A.tw_lo;
     const float2* post = spost;
-    const bool staged = A.staged != 0;
-    const bool last_global = !(A.io_mode == IO_R2C_EVEN || (A.io_mode == IO_C2C && staged));
+    const bool last_global = A.io_mode != IO_R2C_EVEN;
     float2 v[S::E];
+    constexpr int NPP = (L / 2 + 1 + S::NTHR - 1) / S::NTHR;  // C2R pre-process pairs per thread
 
     for (int64_t it = 0;; ++it) {
-        const int64_t slot = gfirst + it * gstride;
-        if (slot >= nslots) break;
+        const int64_t t = gfirst + it * gstride;
+        if (t >= A.ntf) break;
         const int s = (int)(it % NST);
         if (leader && !flags[1 + s]) {
             if (!mbar_wait_bounded(&bars[s], (phase >> s) & 1u)) flags[0] = 1;
@@ -279,115 +292,117 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                 atomicOr(A.err, 1);
                 for (int k = 1; k < NST; ++k) {
                     const int s2 = (s + k) % NST;
-                    const int64_t sl2 = gfirst + (it + k) * gstride;
-                    if (sl2 < nslots && !flags[1 + s2]) mbar_wait_bounded(&bars[s2], (phase >> s2) & 1u);
+                    const int64_t t2 = gfirst + (it + k) * gstride;
+                    if (t2 < A.ntf && !flags[1 + s2]) mbar_wait_bounded(&bars[s2], (phase >> s2) & 1u);
                 }
             }
             break;
         }
-        unsigned char* stg = slots + (int64_t)s * A.stage_bytes;
-        const int64_t t0 = slot * TPS;
-        const int rows = (int)min((int64_t)TPS, A.ntf - t0);
+        const uintptr_t src = buf_lo + (uintptr_t)(t * row_bytes);
+        unsigned char* row = slots + (int64_t)s * A.stage_bytes + (src & 15);
         if (flags[1 + s]) {
-            const unsigned char* src = reinterpret_cast<const unsigned char*>(A.in) + t0 * row_bytes;
-            const int64_t bytes = rows * row_bytes;
-            for (int64_t i = tid; i < bytes / 4; i += S::NTHR)
-                reinterpret_cast<float*>(stg)[i] = __ldg(reinterpret_cast<const float*>(src) + i);
+            const float* gs = reinterpret_cast<const float*>(src);
+            for (int64_t i = tid; i < row_bytes / 4; i += S::NTHR) reinterpret_cast<float*>(row)[i] = __ldg(gs + i);
             group_sync(bar_id, S::NTHR);
         }
-        for (int q = 0; q < rows; ++q) {
-            PipeCtx c;
-            c.L = L;
-            c.nthr = S::NTHR;
-            c.tid = tid;
-            c.ok_sm = true;
-            c.ok_io = true;
-            c.pshift = S::PSHIFT;
-            c.tw = tw;
-            c.sA = W;
-            c.sB = W;
-            c.st2 = reinterpret_cast<const float2*>(stg + (int64_t)q * row_bytes);
-            c.st1 = reinterpret_cast<const float*>(c.st2);
-            c.mode = A.io_mode;
-            c.conj_in = A.conj_in;
-            c.conj_out = A.conj_out;
-            c.weight = A.weight;
-            c.nreal = A.nreal;
-            c.scale = A.scale;
-            const int64_t tt = t0 + q;
-            c.out2 = reinterpret_cast<float2*>(A.out) + tt * A.out_dist;
-            c.out1 = reinterpret_cast<float*>(A.out) + tt * A.out_dist;
+        // work layout (padded, 16-byte aligned) overlaps the raw row: every
+        // pass reads all its inputs before it writes
+        float2* W = reinterpret_cast<float2*>(slots + (int64_t)s * A.stage_bytes + 16);
+        PipeCtx c;
+        c.L = L;
+        c.nthr = S::NTHR;
+        c.tid = tid;
+        c.ok_sm = true;
+        c.ok_io = true;
+        c.pshift = S::PSHIFT;
+        c.tw = tw;
+        c.sA = W;
+        c.sB = W;
+        c.st2 = reinterpret_cast<const float2*>(row);
+        c.st1 = reinterpret_cast<const float*>(row);
+        c.mode = A.io_mode;
+        c.conj_in = A.conj_in;
+        c.conj_out = A.conj_out;
+        c.weight = A.weight;
+        c.nreal = A.nreal;
+        c.scale = A.scale;
+        c.out2 = reinterpret_cast<float2*>(A.out) + t * A.out_dist;
+        c.out1 = reinterpret_cast<float*>(A.out) + t * A.out_dist;
 
-            bool from_slot = true;
-            if (A.io_mode == IO_C2R_EVEN) {
-                // pre-process pairs (k, L-k) from the slot into W:
-                //   Z'[k] = E + i*O,  E = X[k] + conj(X[L-k]),
-                //   O = (X[k] - conj(X[L-k])) * conj(W_N^k), stored conjugated.
-                const bool half = A.weight == WEIGHT_LOAD_HALF;
-                for (int k = tid; k <= (L >> 1); k += S::NTHR) {
-                    if (k == 0) {
-                        const float x0 = c.st2[0].x, xl = c.st2[L].x;  // Im of DC/Nyquist ignored
-                        W[0] = make_float2(x0 + xl, -(x0 - xl));
-                    } else {
-                        float2 a = c.st2[k], b = c.st2[L - k];
-                        if (half) {
-                            a = cscale(a, 0.5f);
-                            b = cscale(b, 0.5f);
-                        }
-                        const float2 w = post[k];
-                        const float2 bc = cconj(b);
-                        const float2 e = cadd(a, bc);
-                        const float2 o = cmulc(csub(a, bc), w);
-                        W[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
-                        if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
-                    }
+        bool from_slot = true;
+        if (A.io_mode == IO_C2R_EVEN) {
+            // pre-process pairs (k, L-k) in place:
+            //   Z'[k] = E + i*O,  E = X[k] + conj(X[L-k]),
+            //   O = (X[k] - conj(X[L-k])) * conj(W_N^k), stored conjugated.
+            // All pairs are read into registers before any is written.
+            const bool half = A.weight == WEIGHT_LOAD_HALF;
+            float2 pa[NPP], pb[NPP];
+            sfor<NPP>([&](auto qq) {
+                constexpr int q = decltype(qq)::value;
+                const int k = tid + q * S::NTHR;
+                if (k <= (L >> 1)) {
+                    pa[q] = c.st2[k];
+                    pb[q] = c.st2[L - k];
                 }
-                group_sync(bar_id, S::NTHR);
-                from_slot = false;
-            }
-            codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, from_slot, last_global, bar_id);
-            // after the slot's last transform has been read, refill the slot
-            if (q == rows - 1 && leader) {
-                const int64_t nsl = gfirst + (it + NST) * gstride;
-                if (nsl < nslots) {
-                    fence_proxy_async_smem();
-                    issue(s, nsl);
-                }
-            }
-            sfor<S::NP - 1>([&](auto pp) {
-                constexpr int P = decltype(pp)::value + 1;
-                codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, false, last_global, bar_id);
             });
-
-            if (A.io_mode == IO_C2C && staged) {
-                for (int i = tid; i < L; i += S::NTHR) {
-                    float2 x = W[cpad<S>(i)];
-                    if (A.conj_out) x = cconj(x);
-                    c.out2[i] = cscale(x, A.scale);
-                }
-                group_sync(bar_id, S::NTHR);
-            } else if (A.io_mode == IO_R2C_EVEN) {
-                // post-process pairs:
-                //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
-                //   X[k] = E + W^k O, X[L-k] = conj(E - W^k O),
-                //   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0 (zero imaginary parts)
-                const float sc = A.scale;
-                const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
-                for (int k = tid; k <= (L >> 1); k += S::NTHR) {
-                    if (k == 0) {
-                        const float2 z0 = W[0];
-                        c.out2[0] = make_float2((z0.x + z0.y) * sc, 0.f);
-                        c.out2[L] = make_float2((z0.x - z0.y) * sc, 0.f);
-                    } else {
-                        const float2 zk = W[cpad<S>(k)], zc = cconj(W[cpad<S>(L - k)]);
-                        const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
-                        const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
-                        const float2 wo = cmul(post[k], o);
-                        c.out2[k] = cscale(cadd(e, wo), s2);
-                        if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
+            group_sync(bar_id, S::NTHR);
+            sfor<NPP>([&](auto qq) {
+                constexpr int q = decltype(qq)::value;
+                const int k = tid + q * S::NTHR;
+                if (k == 0) {
+                    const float x0 = pa[q].x, xl = pb[q].x;  // Im of DC/Nyquist ignored
+                    W[0] = make_float2(x0 + xl, -(x0 - xl));
+                } else if (k <= (L >> 1)) {
+                    float2 a = pa[q], b = pb[q];
+                    if (half) {
+                        a = cscale(a, 0.5f);
+                        b = cscale(b, 0.5f);
                     }
+                    const float2 w = post[k];
+                    const float2 bc = cconj(b);
+                    const float2 e = cadd(a, bc);
+                    const float2 o = cmulc(csub(a, bc), w);
+                    W[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
+                    if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
                 }
-                group_sync(bar_id, S::NTHR);
+            });
+            group_sync(bar_id, S::NTHR);
+            from_slot = false;
+        }
+        codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, from_slot, last_global, bar_id);
+        sfor<S::NP - 1>([&](auto pp) {
+            constexpr int P = decltype(pp)::value + 1;
+            codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, false, last_global, bar_id);
+        });
+        if (A.io_mode == IO_R2C_EVEN) {
+            // post-process pairs:
+            //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
+            //   X[k] = E + W^k O, X[L-k] = conj(E - W^k O),
+            //   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0 (zero imaginary parts)
+            const float sc = A.scale;
+            const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
+            for (int k = tid; k <= (L >> 1); k += S::NTHR) {
+                if (k == 0) {
+                    const float2 z0 = W[0];
+                    c.out2[0] = make_float2((z0.x + z0.y) * sc, 0.f);
+                    c.out2[L] = make_float2((z0.x - z0.y) * sc, 0.f);
+                } else {
+                    const float2 zk = W[cpad<S>(k)], zc = cconj(W[cpad<S>(L - k)]);
+                    const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+                    const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
+                    const float2 wo = cmul(post[k], o);
+                    c.out2[k] = cscale(cadd(e, wo), s2);
+                    if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
+                }
+            }
+            group_sync(bar_id, S::NTHR);
+        }
+        // the slot is free: refill it with the transform NST iterations ahead
+        if (leader) {
+            const int64_t nt = gfirst + (it + NST) * gstride;
+            if (nt < A.ntf) {
+                fence_proxy_async_smem();
+                issue(s, nt);
             }
         }
     }

@@ -97,12 +97,14 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     if ((int64_t)a.tfpc * row_bytes > a.stage_bytes || a.stage_bytes % 16) return fail(why, "row stage too small");
     if (a.codelet >= 0) {
         const int64_t slots_end = 64 + (int64_t)a.nstage * a.stage_bytes;
+        if (a.stage_bytes < a.in_dist * a.in_esize + 32 || a.stage_bytes < 16 + (int64_t)a.lpad * 8 || a.tfpc != 1)
+            return fail(why, "codelet slot too small");
         int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
         gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt);
         if (a.ngroups < 1 || a.ngroups > 15 || a.ngroups * a.ip.nthr > cmaxt) return fail(why, "codelet groups");
         if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
             a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 128 || a.group_bytes % 128 ||
-            a.stage_bytes % 16 || slots_end + (int64_t)a.lpad * 8 > a.group_bytes ||
+            a.stage_bytes % 16 || slots_end > a.group_bytes ||
             a.smem_bytes < a.smem_stage + (int64_t)a.ngroups * a.group_bytes || a.smem_bytes > kMaxSmemBytes)
             return fail(why, "codelet shared-memory layout");
     } else if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||

@@ -210,17 +210,17 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     const int64_t hdr = 128;
     const int64_t tw_bytes = align(tw_cnt * 8, 16);
     const int64_t post_bytes = align(post_cnt * 8, 16);
-    int tps = 1;
-    while ((row_bytes * tps) % 16 != 0 && tps < 16) tps *= 2;
-    const int64_t stage_bytes = align(tps * row_bytes, 16);
-    const int64_t work_bytes = align((int64_t)lpad * 8, 16);
+    const int tps = 1;
+    // one transform per slot: raw row at offset src % 16 (< 16), padded work
+    // layout from offset 16, both inside the slot
+    const int64_t stage_bytes = align(std::max<int64_t>(row_bytes + 32, 16 + (int64_t)lpad * 8), 128);
     const int64_t cta_fixed = align(hdr + tw_bytes + post_bytes, 128);
     const int64_t nslots = (ntf + tps - 1) / tps;
     double best = -1;
     int best_ng = 0, best_ns = 0;
     int64_t best_gb = 0;
     for (int nst = 2; nst <= 3; ++nst) {
-        const int64_t gb = align(64 + nst * stage_bytes + work_bytes, 128);
+        const int64_t gb = align(64 + nst * stage_bytes, 128);
         for (int ng = 1; ng <= 15 && ng * cn <= cmaxt; ++ng) {
             const int64_t smem = cta_fixed + ng * gb;
             if (smem > kMaxSmemBytes) break;
