@@ -66,6 +66,22 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
 ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host, long long maxEntries,
                                           long long* entries);
 
+/* Allocation-free long C2C (no counterpart in the reference).  For callers
+ * that cannot allocate device memory - code running while another component
+ * owns the device memory pool, or that must avoid cudaMalloc/cudaFree and
+ * the synchronisation they may cause.  No plan object: the transform of
+ * `batch` contiguous rows of length nx (nx = L1 * L2, both factors <= 2048
+ * with prime factors <= 47) runs as two column passes whose intermediate is
+ * a fixed 16 MiB device array built into the library, so nx * batch must not
+ * exceed 2^21 (ACLFFT_INVALID_SIZE otherwise).  idata/odata are device
+ * pointers; the call is asynchronous on `stream` and unscaled.  The fixed
+ * arrays are shared by all calls on a device: calls that overlap on the GPU
+ * race.  The first call on each device looks up the arrays' device addresses
+ * (cudaGetSymbolAddress) and should therefore come before any stream
+ * capture. */
+ACLFFT_API aclfftResult aclfftExecC2CNoAlloc(const aclfftComplex* idata, aclfftComplex* odata, int nx, int batch,
+                                             int direction, cudaStream_t stream);
+
 /* Replays the address arithmetic of every launch the plan can make against
  * the buffer sizes of each call variant (no kernel runs).  Returns 0 when
  * all launches stay in bounds; msg receives a description. */

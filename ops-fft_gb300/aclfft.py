@@ -118,6 +118,7 @@ _SIGNATURES = {
     "aclfftGetPlanInfo": [_H, ctypes.POINTER(PlanInfo)],
     "aclfftGetTwiddles": [_H, _VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
     "aclfftDebugCheckPlan": [_H, ctypes.c_char_p, _I],
+    "aclfftExecC2CNoAlloc": [_VP, _VP, _I, _I, _I, _VP],
 }
 
 

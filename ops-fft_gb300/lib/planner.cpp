@@ -543,6 +543,24 @@ std::vector<int> split_axis(int64_t n, int cap)
     return {};
 }
 
+bool build_scratch_c2c_steps(int64_t n, int64_t batch, TwiddleBuilder& tb, std::vector<Step>& out)
+{
+    out.clear();
+    if (n < 2 || batch < 1 || !length_supported(n)) return false;
+    const std::vector<int> fac = split_axis(n, col_max_length());
+    if (fac.size() != 2) return false;
+    Step first, second;
+    if (!make_col_step(n, 1, batch, n, fac[0], 1, tb, first)) return false;
+    if (!make_col_step(n, 1, batch, n, fac[1], fac[0], tb, second)) return false;
+    first.src = BUF_IN;
+    first.dst = BUF_WS;
+    second.src = BUF_WS;
+    second.dst = BUF_OUT;
+    out.push_back(first);
+    out.push_back(second);
+    return true;
+}
+
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
                  int64_t& ws2_bytes)
 {

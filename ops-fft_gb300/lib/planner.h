@@ -86,6 +86,11 @@ struct Problem {
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
                  int64_t& ws2_bytes);
 
+// Two column passes of a long batched C2C (length n = L1 * L2): the first
+// writes its whole output to BUF_WS, the second reads BUF_WS and writes
+// BUF_OUT.  False when n does not split into exactly two on-chip factors.
+bool build_scratch_c2c_steps(int64_t n, int64_t batch, TwiddleBuilder& tb, std::vector<Step>& out);
+
 // Which transform length families are executable (reference domain).
 bool length_supported(int64_t n);
 
