@@ -138,20 +138,11 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
         if (FULL || j < NBF) {
             if constexpr (NS > 1) {
                 const int k = j % NS;
-                const float2* w = tw + tw_off + k * R;
-                if constexpr (R % 2 == 0) {
-                    sfor<R / 2>([&](auto hh) {
-                        constexpr int h = decltype(hh)::value;
-                        const float4 ww = reinterpret_cast<const float4*>(w)[h];
-                        if constexpr (h > 0) v[b * R + 2 * h] = cmul(v[b * R + 2 * h], make_float2(ww.x, ww.y));
-                        v[b * R + 2 * h + 1] = cmul(v[b * R + 2 * h + 1], make_float2(ww.z, ww.w));
-                    });
-                } else {
-                    sfor<R - 1>([&](auto rr) {
-                        constexpr int r = decltype(rr)::value + 1;
-                        v[b * R + r] = cmul(v[b * R + r], w[r]);
-                    });
-                }
+                const float2* w = tw + tw_off + k;  // entry r*NS + k: consecutive k, consecutive banks
+                sfor<R - 1>([&](auto rr) {
+                    constexpr int r = decltype(rr)::value + 1;
+                    v[b * R + r] = cmul(v[b * R + r], w[r * NS]);
+                });
             }
             DFT<R>::run(&v[b * R]);
         }

@@ -16,9 +16,9 @@ __global__ void twiddle_kernel(float2* __restrict__ out, TwSeg seg)
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < seg.count; i += stride) {
         int64_t m;
-        if (seg.kind == 0) {
-            const int64_t R = seg.R_or_mult;
-            m = ((i / R) * (i % R)) % seg.M;
+        if (seg.kind == 2) {
+            const int64_t ns = seg.R_or_mult;
+            m = ((i / ns) * (i % ns)) % seg.M;
         } else {
             m = (int64_t)(((unsigned __int128)i * (unsigned __int128)seg.R_or_mult) % (unsigned __int128)seg.M);
         }

@@ -12,8 +12,8 @@ constexpr int kMaxSmemBytes = 227 * 1024;
 
 // One on-chip Stockham pass: radix R after a product `ns` of earlier radices.
 // Butterfly j reads x[j + r*L/R] and writes y[(j/ns)*ns*R + j%ns + r*ns]
-// after multiplying input r by W_{ns*R}^{(j%ns)*r} (table at tw_off, rows of
-// R entries, one row per j%ns).
+// after multiplying input r by W_{ns*R}^{(j%ns)*r}, read from the table at
+// tw_off, entry r*ns + j%ns.
 struct PassDesc {
     int32_t radix;
     int32_t ns;
@@ -128,8 +128,8 @@ struct PackArgs {
 };
 
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
-//   kind 0: f(i) = ((i / R) * (i % R)) mod M      (pass tables, rows of R)
 //   kind 1: f(i) = (i * mult) mod M               (linear tables)
+//   kind 2: f(i) = ((i / ns) * (i % ns)) mod M    (pass tables, [r][k] layout)
 struct TwSeg {
     int64_t offset;  // float2 offset in the table blob
     int64_t count;

@@ -81,20 +81,11 @@ __device__ __forceinline__ void stockham_pass(const Ctx& c, const PassDesc& pd, 
         if (pd.ns > 1) {
             const int q = fdiv(j, pd);
             const int k = j - q * pd.ns;
-            const float2* w = c.tw + pd.tw_off + k * R;
-            if constexpr (R % 2 == 0) {
-                sfor<R / 2>([&](auto hh) {
-                    constexpr int h = decltype(hh)::value;
-                    const float4 ww = reinterpret_cast<const float4*>(w)[h];  // shared or global (generic load)
-                    if constexpr (h > 0) u[2 * h] = cmul(u[2 * h], make_float2(ww.x, ww.y));
-                    u[2 * h + 1] = cmul(u[2 * h + 1], make_float2(ww.z, ww.w));
-                });
-            } else {
-                sfor<R - 1>([&](auto rr) {
-                    constexpr int r = decltype(rr)::value + 1;
-                    u[r] = cmul(u[r], w[r]);
-                });
-            }
+            const float2* w = c.tw + pd.tw_off + k;  // entry r*ns + k
+            sfor<R - 1>([&](auto rr) {
+                constexpr int r = decltype(rr)::value + 1;
+                u[r] = cmul(u[r], w[r * pd.ns]);
+            });
         }
         DFT<R>::run(u);
         if (dst == 0) {

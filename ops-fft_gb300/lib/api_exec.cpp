@@ -111,6 +111,74 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
     return 0;
 }
 
+// Host buffers, one row-kernel step: the batch is cut into chunks whose
+// host-to-device copy, kernel and device-to-host copy run on three streams,
+// so copies in both directions overlap the kernels of neighbouring chunks.
+// Returns 0 on success, 1 on failure, -1 when the transform is too small to
+// be worth chunking (the caller then runs the plain staged path).
+int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* out, size_t in_bytes,
+                        size_t out_bytes, cudaStream_t st, bool c2c, bool inverse, float scale)
+{
+    const int64_t ntf = step.row.ntf;
+    constexpr int kChunks = 8;
+    if (ntf < 2 * kChunks || in_bytes + out_bytes < (size_t)(8u << 20)) return -1;
+    if (in_bytes % (size_t)ntf || out_bytes % (size_t)ntf) return -1;
+    const size_t rin = in_bytes / (size_t)ntf, rout = out_bytes / (size_t)ntf;
+    if (!impl->pipe_ready) {
+        bool ok = cudaStreamCreateWithFlags(&impl->s_in, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaStreamCreateWithFlags(&impl->s_out, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&impl->ev_start, cudaEventDisableTiming) == cudaSuccess;
+        for (int c = 0; ok && c < kChunks; ++c)
+            ok = cudaEventCreateWithFlags(&impl->ev_in[c], cudaEventDisableTiming) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&impl->ev_k[c], cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
+            cudaGetLastError();
+            return -1;
+        }
+        impl->pipe_ready = true;
+    }
+    if (cudaEventRecord(impl->ev_start, st) != cudaSuccess || cudaStreamWaitEvent(impl->s_in, impl->ev_start, 0) != cudaSuccess)
+        return 1;
+    const int64_t per = (ntf + kChunks - 1) / kChunks;
+    const float2* tw = static_cast<const float2*>(impl->tw);
+    int used = 0;
+    for (int c = 0; c < kChunks; ++c) {
+        const int64_t t0 = c * per, t1 = std::min<int64_t>(ntf, t0 + per);
+        if (t0 >= t1) break;
+        ++used;
+        char* din = static_cast<char*>(impl->stage_a) + t0 * rin;
+        char* dout = static_cast<char*>(impl->stage_b) + t0 * rout;
+        if (cudaMemcpyAsync(din, static_cast<const char*>(in) + t0 * rin, (t1 - t0) * rin, cudaMemcpyHostToDevice,
+                            impl->s_in) != cudaSuccess ||
+            cudaEventRecord(impl->ev_in[c], impl->s_in) != cudaSuccess ||
+            cudaStreamWaitEvent(st, impl->ev_in[c], 0) != cudaSuccess)
+            return 1;
+        gfft::RowArgs a = step.row;
+        a.tw = tw;
+        a.post_tw = step.post_off >= 0 ? tw + step.post_off : nullptr;
+        a.in = din;
+        a.out = dout;
+        a.err = impl->err;
+        a.ntf = t1 - t0;
+        if (c2c) {
+            a.conj_in = inverse;
+            a.conj_out = inverse;
+        }
+        a.scale = scale;
+        if (gfft_launch_row(&a, st) != 0 || cudaEventRecord(impl->ev_k[c], st) != cudaSuccess ||
+            cudaStreamWaitEvent(impl->s_out, impl->ev_k[c], 0) != cudaSuccess ||
+            cudaMemcpyAsync(static_cast<char*>(out) + t0 * rout, dout, (t1 - t0) * rout, cudaMemcpyDeviceToHost,
+                            impl->s_out) != cudaSuccess)
+            return 1;
+    }
+    (void)used;
+    if (cudaStreamSynchronize(impl->s_out) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return 0;
+}
+
 struct CallShape {
     size_t in_bytes;
     size_t out_bytes;
@@ -169,6 +237,11 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     }
     void* dev_in = din ? in : impl->stage_a;
     void* dev_out = dout ? out : impl->stage_b;
+    if (!din && !dout && primary.steps.size() == 1 && primary.steps[0].kind == Step::ROW) {
+        const int rc = exec_host_pipelined(impl, primary.steps[0], in, out, shape.in_bytes, shape.out_bytes, st, c2c,
+                                           inverse, scale);
+        if (rc >= 0) return rc == 0 ? ACLFFT_SUCCESS : ACLFFT_EXEC_FAILED;
+    }
     if (!din && cudaMemcpyAsync(dev_in, in, shape.in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         cudaGetLastError();
         return ACLFFT_EXEC_FAILED;

@@ -140,6 +140,16 @@ void plan_impl_free(PlanImpl* p)
     if (p->stage_b) cudaFree(p->stage_b);
     if (p->err) cudaFree(p->err);
     p->err = nullptr;
+    if (p->pipe_ready) {
+        cudaStreamDestroy(p->s_in);
+        cudaStreamDestroy(p->s_out);
+        cudaEventDestroy(p->ev_start);
+        for (int c = 0; c < 8; ++c) {
+            cudaEventDestroy(p->ev_in[c]);
+            cudaEventDestroy(p->ev_k[c]);
+        }
+        p->pipe_ready = false;
+    }
     p->tw = p->ws = p->ws2 = p->stage_a = p->stage_b = nullptr;
     p->device_ready = false;
 }

@@ -37,6 +37,12 @@ struct PlanImpl {
     void* stage_a = nullptr;
     void* stage_b = nullptr;
     size_t stage_bytes = 0;
+    // chunked host pipeline (created on the first exec with host buffers)
+    bool pipe_ready = false;
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_start = nullptr;
+    cudaEvent_t ev_in[8] = {};
+    cudaEvent_t ev_k[8] = {};
 };
 
 void plan_impl_free(PlanImpl* p);

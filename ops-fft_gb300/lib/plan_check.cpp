@@ -40,7 +40,7 @@ bool check_inner(const InnerPlan& ip, int64_t tw_count, std::string& why)
         if (d.ns != ns) return fail(why, "ns mismatch");
         if (ns > 1) {
             if (d.tw_off < 0 || d.tw_off + ns * d.radix > tw_count) return fail(why, "pass twiddle out of table");
-            if (d.radix % 2 == 0 && (d.tw_off % 2) != 0) return fail(why, "pass twiddle misaligned for float4");
+
             if (ns >= 65536 || ip.L >= 65536) return fail(why, "fast division range exceeded");
             // verify the magic division for every j that occurs
             const int nbf = ip.L / d.radix;

@@ -83,15 +83,17 @@ std::vector<int> choose_radices(int L)
 
 int64_t TwiddleBuilder::add_pass_table(int64_t ns, int R)
 {
+    // layout [r][k]: entry r*ns + k = W_{ns*R}^{k*r}; consecutive butterflies
+    // (consecutive k) read consecutive entries
     for (const TwSeg& t : segs)
-        if (t.kind == 0 && t.M == ns * R && t.R_or_mult == R) return t.offset;
+        if (t.kind == 2 && t.M == ns * R && t.R_or_mult == ns) return t.offset;
     const int64_t off = count;
     TwSeg s{};
     s.offset = off;
     s.count = ns * R;
     s.M = ns * R;
-    s.R_or_mult = R;
-    s.kind = 0;
+    s.R_or_mult = ns;
+    s.kind = 2;
     segs.push_back(s);
     count += ns * R;
     count += count & 1;
