@@ -97,19 +97,80 @@ struct W {
 };
 
 // ------------------------------------------------------ complex helpers
-GFFT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-GFFT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// On sm_100+ device code the helpers use the paired FP32 instructions
+// (one FADD2/FMUL2/FFMA2 per complex op instead of two scalar ops).  Each
+// lane of a paired op rounds exactly like the scalar op it replaces, so
+// results are bit-identical to the scalar host forms below.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000) && !defined(GFFT_SCALAR_COMPLEX)
+#define GFFT_PAIRED 1
+#endif
+
+GFFT_HD float2 cadd(float2 a, float2 b)
+{
+#ifdef GFFT_PAIRED
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+GFFT_HD float2 csub(float2 a, float2 b)
+{
+#ifdef GFFT_PAIRED
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 GFFT_HD float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
-GFFT_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+GFFT_HD float2 cscale(float2 a, float s)
+{
+#ifdef GFFT_PAIRED
+    return __fmul2_rn(a, make_float2(s, s));
+#else
+    return make_float2(a.x * s, a.y * s);
+#endif
+}
+// (re, im) = (a.x*b.x - a.y*b.y, a.x*b.y + a.y*b.x), the products a.y*b
+// rounded first and the a.x*b terms fused.
 GFFT_HD float2 cmul(float2 a, float2 b)
 {
+#ifdef GFFT_PAIRED
+    const float2 t = __fmul2_rn(make_float2(a.y, a.y), make_float2(b.y, b.x));
+    return __ffma2_rn(make_float2(a.x, a.x), b, make_float2(-t.x, t.y));
+#else
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+#endif
 }
-// a * conj(b)
+// a * conj(b) = (a.x*b.x + a.y*b.y, a.y*b.x - a.x*b.y)
 GFFT_HD float2 cmulc(float2 a, float2 b)
 {
+#ifdef GFFT_PAIRED
+    const float2 t = __fmul2_rn(make_float2(a.y, a.x), make_float2(b.y, b.y));
+    return __ffma2_rn(make_float2(a.x, a.y), make_float2(b.x, b.x), make_float2(t.x, -t.y));
+#else
     return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+#endif
 }
+// acc + s * a per component (fused).
+GFFT_HD float2 sfma(float s, float2 a, float2 acc)
+{
+#ifdef GFFT_PAIRED
+    return __ffma2_rn(make_float2(s, s), a, acc);
+#else
+    return make_float2(fmaf(s, a.x, acc.x), fmaf(s, a.y, acc.y));
+#endif
+}
+// a * b per component.
+GFFT_HD float2 pmul(float2 a, float2 b)
+{
+#ifdef GFFT_PAIRED
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+// (a + b) * h per component (the odd multiples of pi/4 rotations).
+GFFT_HD float2 sum_scale(float2 a, float2 b, float h) { return cscale(cadd(a, b), h); }
 GFFT_HD float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // * (-i)
 GFFT_HD float2 mul_pi(float2 a) { return make_float2(-a.y, a.x); }  // * (+i)
 
@@ -127,20 +188,15 @@ GFFT_HD float2 twc(float2 x)
     } else if constexpr (4 * e == 3 * R) {
         return mul_pi(x);
     } else if constexpr (8 * e == R) {
-        constexpr float h = W<8, 1>::re;  // sqrt(1/2)
-        return make_float2((x.x + x.y) * h, (x.y - x.x) * h);
+        return sum_scale(make_float2(x.x, x.y), make_float2(x.y, -x.x), W<8, 1>::re);
     } else if constexpr (8 * e == 3 * R) {
-        constexpr float h = W<8, 1>::re;
-        return make_float2((x.y - x.x) * h, -(x.x + x.y) * h);
+        return sum_scale(make_float2(x.y, -x.x), make_float2(-x.x, -x.y), W<8, 1>::re);
     } else if constexpr (8 * e == 5 * R) {
-        constexpr float h = W<8, 1>::re;
-        return make_float2(-(x.x + x.y) * h, (x.x - x.y) * h);
+        return sum_scale(make_float2(-x.x, x.x), make_float2(-x.y, -x.y), W<8, 1>::re);
     } else if constexpr (8 * e == 7 * R) {
-        constexpr float h = W<8, 1>::re;
-        return make_float2((x.x - x.y) * h, (x.x + x.y) * h);
+        return sum_scale(make_float2(x.x, x.x), make_float2(-x.y, x.y), W<8, 1>::re);
     } else {
-        constexpr float c = W<R, e>::re, s = W<R, e>::im;
-        return make_float2(fmaf(x.x, c, -x.y * s), fmaf(x.x, s, x.y * c));
+        return cmul(x, make_float2(W<R, e>::re, W<R, e>::im));
     }
 }
 
@@ -184,9 +240,9 @@ struct DFT<3> {
     {
         constexpr float s3 = float(0.86602540378443864676372317075294);  // sin(2pi/3)
         const float2 t1 = cadd(v[1], v[2]);
-        const float2 t2 = make_float2(fmaf(-0.5f, t1.x, v[0].x), fmaf(-0.5f, t1.y, v[0].y));
+        const float2 t2 = sfma(-0.5f, t1, v[0]);
         const float2 d = csub(v[1], v[2]);
-        const float2 t3 = make_float2(s3 * d.y, -s3 * d.x);  // -i*s3*(v1-v2)
+        const float2 t3 = pmul(make_float2(s3, -s3), make_float2(d.y, d.x));  // -i*s3*(v1-v2)
         v[0] = cadd(v[0], t1);
         v[1] = cadd(t2, t3);
         v[2] = csub(t2, t3);
@@ -230,14 +286,12 @@ struct DFT<P, std::enable_if_t<(P >= 5) && is_prime(P)>> {
                 constexpr int j = decltype(jj)::value + 1;
                 constexpr Root rt = unit_root((long long)j * k, P);
                 constexpr float c = float(rt.c), s = float(rt.s);
-                re.x = fmaf(c, A[j - 1].x, re.x);
-                re.y = fmaf(c, A[j - 1].y, re.y);
-                im.x = fmaf(s, B[j - 1].x, im.x);
-                im.y = fmaf(s, B[j - 1].y, im.y);
+                re = sfma(c, A[j - 1], re);
+                im = sfma(s, B[j - 1], im);
             });
             // X_k = re - i*im ; X_{P-k} = re + i*im
-            v[k] = make_float2(re.x + im.y, re.y - im.x);
-            v[P - k] = make_float2(re.x - im.y, re.y + im.x);
+            v[k] = cadd(re, make_float2(im.y, -im.x));
+            v[P - k] = cadd(re, make_float2(-im.y, im.x));
         });
     }
 };

@@ -110,9 +110,20 @@ __device__ __forceinline__ void stockham_pass(const Ctx& c, const PassDesc& pd, 
     __syncthreads();
 }
 
-#define GFFT_RADIX_CASE(RV)                             \
-    case RV:                                            \
-        if constexpr (RV <= RMAX) stockham_pass<RV>(c, pd, src, dst); \
+// Passes of the large primes (17..47) are rare; keeping them out of line
+// keeps the radix-47 kernels' code size and compile time bounded.
+template <int R, class Ctx>
+__device__ __noinline__ void stockham_pass_outlined(const Ctx& c, const PassDesc& pd, int src, int dst)
+{
+    stockham_pass<R>(c, pd, src, dst);
+}
+
+#define GFFT_RADIX_CASE(RV)                                                 \
+    case RV:                                                                \
+        if constexpr (RV <= RMAX) {                                         \
+            if constexpr (RV > 16) stockham_pass_outlined<RV>(c, pd, src, dst); \
+            else stockham_pass<RV>(c, pd, src, dst);                        \
+        }                                                                   \
         break;
 
 // Runs all passes.  `start` is where the data is (0 = HBM, 1 = buffer A);
