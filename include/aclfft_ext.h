@@ -29,6 +29,27 @@ typedef enum aclfftNormMode_t {
 ACLFFT_API aclfftResult aclfftSetNormMode(aclfftHandle plan, int normMode);
 ACLFFT_API aclfftResult aclfftGetNormMode(aclfftHandle plan, int* normMode);
 
+/* Arithmetic of the C2C DFT stages.  ACLFFT_PREC_FP32 (default) runs the
+ * FP32 Stockham kernels.  The split-precision forms run the on-chip
+ * 64- and 256-point sub-transforms as tensor-core DFT-matrix stages (8- and
+ * 16-point real-embedded DFT matrices on tcgen05) with both the data and the
+ * matrices split into hi + lo parts of the operand type and three products
+ * accumulated in FP32: TF32x3 keeps plain-FP32 accuracy, BF16x3 about 1e-5
+ * relative.  They apply to 1D HORIZONTAL C2C plans of length 64, 256, or a
+ * product of two of {64, 256} (4096, 16384, 65536); other plans keep the
+ * FP32 kernels (aclfftGetPlanInfo reports which ran via tc_stages).
+ * Settable before or after MakePlan (a made plan is re-planned; returns
+ * ACLFFT_ALLOC_FAILED / ACLFFT_SETUP_FAILED if that fails, leaving the old
+ * plan in place).  The mode is not part of the reference API. */
+typedef enum aclfftPrecisionMode_t {
+    ACLFFT_PREC_FP32 = 0,
+    ACLFFT_PREC_TF32X3 = 1,
+    ACLFFT_PREC_BF16X3 = 2
+} aclfftPrecisionMode;
+
+ACLFFT_API aclfftResult aclfftSetPrecisionMode(aclfftHandle plan, int mode);
+ACLFFT_API aclfftResult aclfftGetPrecisionMode(aclfftHandle plan, int* mode);
+
 /* Adjoint (vector-Jacobian) transforms, using the complex-gradient convention
  * g = dL/dRe + i dL/dIm.  Same pointer and stream semantics as the Exec
  * calls; the plan's normalisation scale carries over unchanged.
@@ -57,6 +78,7 @@ typedef struct aclfftPlanInfo_t {
     int groups_per_cta;        /* codelets: independent transform groups per CTA */
     int stages;                /* input prefetch stages */
     int smem_bytes;            /* dynamic shared memory per CTA */
+    int tc_stages;             /* tensor-core DFT-matrix launches per exec (0: FP32 kernels only) */
 } aclfftPlanInfo;
 
 ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info);

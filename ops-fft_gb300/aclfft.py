@@ -52,6 +52,11 @@ NORM_BACKWARD = 1
 NORM_ORTHO = 2
 NORM_FORWARD = 3
 
+# aclfftPrecisionMode (C2C DFT-stage arithmetic)
+PREC_FP32 = 0
+PREC_TF32X3 = 1
+PREC_BF16X3 = 2
+
 
 class PlanInfo(ctypes.Structure):
     _fields_ = [
@@ -68,6 +73,7 @@ class PlanInfo(ctypes.Structure):
         ("groups_per_cta", ctypes.c_int),
         ("stages", ctypes.c_int),
         ("smem_bytes", ctypes.c_int),
+        ("tc_stages", ctypes.c_int),
     ]
 
 
@@ -112,6 +118,8 @@ _SIGNATURES = {
     "aclfftGetProperty": [_I, ctypes.POINTER(_I)],
     "aclfftSetNormMode": [_H, _I],
     "aclfftGetNormMode": [_H, ctypes.POINTER(_I)],
+    "aclfftSetPrecisionMode": [_H, _I],
+    "aclfftGetPrecisionMode": [_H, ctypes.POINTER(_I)],
     "aclfftExecC2CAdjoint": [_H, _VP, _VP, _I],
     "aclfftExecR2CAdjoint": [_H, _VP, _VP],
     "aclfftExecC2RAdjoint": [_H, _VP, _VP],
@@ -193,6 +201,15 @@ class Plan:
 
     def set_norm(self, mode: int) -> None:
         _check(lib().aclfftSetNormMode(self.handle, mode), "aclfftSetNormMode")
+
+    def set_precision(self, mode: int) -> None:
+        """PREC_FP32 (Stockham), PREC_TF32X3 or PREC_BF16X3 (tensor-core DFT stages)."""
+        _check(lib().aclfftSetPrecisionMode(self.handle, mode), "aclfftSetPrecisionMode")
+
+    def precision(self) -> int:
+        m = _I()
+        _check(lib().aclfftGetPrecisionMode(self.handle, ctypes.byref(m)), "aclfftGetPrecisionMode")
+        return m.value
 
     def exec_c2c(self, x, y, direction: int = FORWARD) -> None:
         _check(lib().aclfftExecC2C(self.handle, ptr(x), ptr(y), direction), "aclfftExecC2C")

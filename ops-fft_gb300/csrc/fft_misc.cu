@@ -130,6 +130,12 @@ extern "C" int gfft_gen_twiddles(void* table, const TwSeg* segs, int nseg, void*
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int i = 0; i < nseg; ++i) {
         if (segs[i].count <= 0) continue;
+        if (segs[i].kind == 3) {
+            const int rc = gfft_tc_gen_bmat(static_cast<float2*>(table) + segs[i].offset, (int)segs[i].M,
+                                            (int)segs[i].R_or_mult, stream);
+            if (rc != 0) return rc;
+            continue;
+        }
         const int64_t blocks64 = (segs[i].count + 255) / 256;
         const unsigned blocks = (unsigned)(blocks64 > 4096 ? 4096 : blocks64);
         twiddle_kernel<<<blocks, 256, 0, st>>>(static_cast<float2*>(table), segs[i]);

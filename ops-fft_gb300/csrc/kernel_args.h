@@ -127,9 +127,48 @@ struct PackArgs {
     float scale;
 };
 
+// Split-precision tensor-core sub-transforms of length L = R*R (R = 8 or
+// 16): two DFT-matrix stages (R-point DFTs as [128 x 2R] x [2R x 2R] real
+// GEMMs on tcgen05, operands split hi + lo, three products) with the W_L
+// twiddle between them.  Sequence q = b*S + s, element n at
+// in[b*in_dist + s*in_s + n*in_n]; output bin k at the same form with out_*,
+// multiplied by W_N^{s*k} (N = S*L) when otw_hi is set.
+enum TcIo : int32_t {
+    TC_IO_GENERIC = 0,      // any strides (8-byte accesses)
+    TC_IO_INTERLEAVED = 1,  // s stride 1: consecutive sequences side by side
+    TC_IO_CONTIG = 2,       // n stride 1: each sequence contiguous
+};
+enum TcPrec : int32_t { TC_PREC_TF32X3 = 1, TC_PREC_BF16X3 = 2 };
+
+struct TcArgs {
+    const void* in;
+    void* out;
+    const void* bmat;    // DFT-matrix operand images (hi, then lo) in core-matrix layout
+    const void* twl;     // W_L^j, j < L
+    const void* otw_hi;  // W_N^{(e >> otw_shift) << otw_shift}; nullptr: no outer twiddle
+    const void* otw_lo;  // W_N^{e & mask}
+    int* err;
+    int64_t nseq;
+    int64_t S;
+    int64_t in_dist, in_s, in_n;
+    int64_t out_dist, out_s, out_n;
+    int32_t R;
+    int32_t prec;
+    int32_t in_mode;
+    int32_t out_mode;
+    int32_t otw_shift;
+    int32_t otw_hi_n;
+    int32_t otw_lo_n;
+    int32_t conj_in;
+    int32_t conj_out;
+    float scale;
+};
+
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
 //   kind 1: f(i) = (i * mult) mod M               (linear tables)
 //   kind 2: f(i) = ((i / ns) * (i % ns)) mod M    (pass tables, [r][k] layout)
+//   kind 3: the hi and lo operand images of the real-embedded R-point DFT
+//           matrix (M = R, R_or_mult = TcPrec) for the tensor-core stages
 struct TwSeg {
     int64_t offset;  // float2 offset in the table blob
     int64_t count;
@@ -146,6 +185,10 @@ extern "C" {
 int gfft_launch_row(const gfft::RowArgs* a, void* stream);
 int gfft_launch_col(const gfft::ColArgs* a, void* stream);
 int gfft_launch_pack(const gfft::PackArgs* a, void* stream);
+int gfft_launch_tc(const gfft::TcArgs* a, void* stream);
+// float2 entries of the two DFT-matrix operand images for (R, prec).
+long long gfft_tc_bmat_entries(int R, int prec);
+int gfft_tc_gen_bmat(void* dst, int R, int prec, void* stream);
 int gfft_gen_twiddles(void* table, const gfft::TwSeg* segs, int nseg, void* stream);
 int gfft_kernel_max_threads(int rmax);
 // Compile-time specialised row kernel for length L: returns its id (or -1)

@@ -101,6 +101,21 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
         case Step::COPY:
             rc = (int)cudaMemcpyAsync(dst, src, (size_t)s.copy_bytes, cudaMemcpyDeviceToDevice, st);
             break;
+        case Step::TC:
+            s.tc.in = src;
+            s.tc.out = dst;
+            s.tc.bmat = tw + s.bmat_off;
+            s.tc.twl = tw + s.tw_off;
+            s.tc.otw_hi = s.hi_off >= 0 ? tw + s.hi_off : nullptr;
+            s.tc.otw_lo = s.lo_off >= 0 ? tw + s.lo_off : nullptr;
+            s.tc.err = impl->err;
+            if (c2c) {
+                s.tc.conj_in = first && inverse;
+                s.tc.conj_out = last && inverse;
+            }
+            if (last) s.tc.scale = scale;
+            rc = gfft_launch_tc(&s.tc, st);
+            break;
         }
         if (rc != 0) {
             gfft::set_last_error(std::string("kernel launch failed: ") + cudaGetErrorString((cudaError_t)rc));

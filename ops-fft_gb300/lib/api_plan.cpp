@@ -93,6 +93,7 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
     pr.n1 = h->rank == 2 ? h->lengths[1] : 1;
     pr.batch = h->batch;
     pr.stride = h->rank == 1 ? h->stride[0] : 1;
+    pr.prec = pr.kind == Kind::C2C && pr.rank == 1 ? h->precision : 0;
     impl->prob = pr;
     Problem adj = pr;
     if (pr.kind == Kind::R2C) {
@@ -114,14 +115,17 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
         gfft::set_last_error("internal planning failure");
         return ACLFFT_INTERNAL_ERROR;
     }
-    h->impl = impl;
     const aclfftResult r = gfft::plan_device_setup(impl);
     if (r != ACLFFT_SUCCESS) {
         gfft::plan_impl_free(impl);
         delete impl;
-        h->impl = nullptr;
         return r;
     }
+    if (h->impl) {  // re-plan of a made plan: the new state replaces the old
+        gfft::plan_impl_free(h->impl);
+        delete h->impl;
+    }
+    h->impl = impl;
     if (workSize) *workSize = (size_t)(impl->ws_bytes + impl->ws2_bytes);
     return ACLFFT_SUCCESS;
 }
@@ -129,6 +133,23 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
 }  // namespace
 
 namespace gfft {
+
+aclfftResult replan(aclfftHandle_t* h)
+{
+    if (!h->is_initialized || !h->impl) return ACLFFT_SUCCESS;
+    const int dev = h->impl->device;
+    int cur = -1;
+    if (h->impl->device_ready && cudaGetDevice(&cur) == cudaSuccess && cur != dev) {
+        if (cudaSetDevice(dev) != cudaSuccess) {
+            cudaGetLastError();
+            return ACLFFT_INVALID_DEVICE;
+        }
+        const aclfftResult r = plan_execution(h, nullptr);
+        cudaSetDevice(cur);
+        return r;
+    }
+    return plan_execution(h, nullptr);
+}
 
 void plan_impl_free(PlanImpl* p)
 {

@@ -111,6 +111,26 @@ ACLFFT_API aclfftResult aclfftSetNormMode(aclfftHandle plan, int normMode)
     return ACLFFT_SUCCESS;
 }
 
+ACLFFT_API aclfftResult aclfftSetPrecisionMode(aclfftHandle plan, int mode)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_PARAM(mode >= ACLFFT_PREC_FP32 && mode <= ACLFFT_PREC_BF16X3, ACLFFT_INVALID_VALUE);
+    if (plan->precision == mode) return ACLFFT_SUCCESS;
+    const int old = plan->precision;
+    plan->precision = mode;
+    const aclfftResult r = gfft::replan(plan);
+    if (r != ACLFFT_SUCCESS) plan->precision = old;
+    return r;
+}
+
+ACLFFT_API aclfftResult aclfftGetPrecisionMode(aclfftHandle plan, int* mode)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(mode);
+    *mode = plan->precision;
+    return ACLFFT_SUCCESS;
+}
+
 ACLFFT_API aclfftResult aclfftGetNormMode(aclfftHandle plan, int* normMode)
 {
     ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
@@ -128,6 +148,8 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
     const gfft::StepList& sl = plan->impl->lists[0];
     info->supported = sl.supported ? 1 : 0;
     info->nsteps = (int)sl.steps.size();
+    for (const gfft::Step& s : sl.steps)
+        if (s.kind == gfft::Step::TC) ++info->tc_stages;
     for (const gfft::Step& s : sl.steps) {
         const gfft::InnerPlan* ip = nullptr;
         int tf = 0;

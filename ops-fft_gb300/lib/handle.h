@@ -17,6 +17,8 @@
 #include "../../include/cann_ops_fft.h"
 #include "planner.h"
 
+struct aclfftHandle_t;
+
 namespace gfft {
 
 struct PlanImpl {
@@ -46,6 +48,9 @@ struct PlanImpl {
 };
 
 void plan_impl_free(PlanImpl* p);
+// Rebuilds a made plan after a setting that changes its steps; the old
+// state is kept on failure.
+aclfftResult replan(aclfftHandle_t* h);
 aclfftResult plan_device_setup(PlanImpl* p);
 
 void set_last_error(const std::string& s);
@@ -63,10 +68,11 @@ struct aclfftHandle_t {
     cudaStream_t stream;
     bool is_initialized;
     gfft::PlanImpl* impl;
+    int32_t precision;  // aclfftPrecisionMode (extension)
 
     aclfftHandle_t()
         : rank(0), lengths{0, 0, 0}, stride{0, 0, 0}, batch(1), type(ACLFFT_C2C), normMode(0), stream(nullptr),
-          is_initialized(false), impl(nullptr)
+          is_initialized(false), impl(nullptr), precision(0)
     {
     }
     ~aclfftHandle_t()

@@ -197,6 +197,58 @@ bool check_pack(const Step& s, const Bufs& b, int64_t tw_count, std::string& why
 
 }  // namespace
 
+namespace {
+
+// Tensor-core pass: every tile's HBM accesses, 16-byte alignment of the
+// vector modes, the batch item shared by a tile and the table ranges.
+bool check_tc(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
+{
+    const TcArgs& a = s.tc;
+    if (a.R != 8 && a.R != 16) return fail(why, "tc radix");
+    if (a.prec != TC_PREC_TF32X3 && a.prec != TC_PREC_BF16X3) return fail(why, "tc precision");
+    const int64_t L = (int64_t)a.R * a.R, TS = 128 / a.R;
+    if (a.nseq < 1 || a.S < 1) return fail(why, "tc sizes");
+    if (a.S % TS != 0 && a.S < a.nseq) return fail(why, "tc tile spans two batch items");
+    const int64_t ein = b.bytes[s.src] / 8, eout = b.bytes[s.dst] / 8;
+    auto mode_ok = [&](int mode, int64_t dist, int64_t ss, int64_t sn) {
+        if (mode == TC_IO_INTERLEAVED)
+            return ss == 1 && dist % 2 == 0 && sn % 2 == 0 && a.S % TS == 0 && a.nseq % TS == 0;
+        if (mode == TC_IO_CONTIG) return sn == 1 && dist % 2 == 0 && ss % 2 == 0;
+        return mode == TC_IO_GENERIC;
+    };
+    if (!mode_ok(a.in_mode, a.in_dist, a.in_s, a.in_n)) return fail(why, "tc input mode");
+    if (!mode_ok(a.out_mode, a.out_dist, a.out_s, a.out_n)) return fail(why, "tc output mode");
+    if (a.in_dist < 0 || a.in_s < 0 || a.in_n < 0 || a.out_dist < 0 || a.out_s < 0 || a.out_n < 0)
+        return fail(why, "tc negative stride");
+    const int64_t ntiles = (a.nseq + TS - 1) / TS;
+    for (int64_t t = 0; t < ntiles; ++t) {
+        const int64_t q0 = t * TS;
+        const int64_t nv = std::min<int64_t>(TS, a.nseq - q0);
+        const int64_t bi = q0 / a.S, s0 = q0 - bi * a.S;
+        if ((q0 + nv - 1) / a.S != bi) return fail(why, "tc tile spans two batch items");
+        const int64_t hi_in = bi * a.in_dist + (s0 + nv - 1) * a.in_s + (L - 1) * a.in_n;
+        const int64_t hi_out = bi * a.out_dist + (s0 + nv - 1) * a.out_s + (L - 1) * a.out_n;
+        if (hi_in >= ein) return fail(why, "tc load out of bounds");
+        if (hi_out >= eout) return fail(why, "tc store out of bounds");
+        if (a.in_mode == TC_IO_INTERLEAVED && (s0 % 2 != 0 || nv != TS)) return fail(why, "tc interleaved tile");
+        if (a.out_mode == TC_IO_INTERLEAVED && (s0 % 2 != 0 || nv != TS)) return fail(why, "tc interleaved tile");
+    }
+    if (s.bmat_off < 0 || s.bmat_off % 2 || s.bmat_off + gfft_tc_bmat_entries(a.R, a.prec) > tw_count)
+        return fail(why, "tc matrix images out of table");
+    if (s.tw_off < 0 || s.tw_off + L > tw_count) return fail(why, "tc twiddles out of table");
+    if (s.hi_off >= 0) {
+        if (s.lo_off < 0 || a.otw_shift < 0 || a.otw_shift > 20) return fail(why, "tc outer twiddle");
+        if (s.hi_off + a.otw_hi_n > tw_count || s.lo_off + a.otw_lo_n > tw_count)
+            return fail(why, "tc outer twiddle out of table");
+        const int64_t emax = (a.S - 1) * (L - 1);
+        if ((emax >> a.otw_shift) >= a.otw_hi_n || a.otw_lo_n != (1 << a.otw_shift))
+            return fail(why, "tc outer twiddle index range");
+    }
+    return true;
+}
+
+}  // namespace
+
 extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int msglen)
 {
     auto report = [&](const std::string& s) {
@@ -244,6 +296,7 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
             else if (s.kind == Step::ROW) ok = check_row(s, b, impl->tb.count, why);
             else if (s.kind == Step::COL) ok = check_col(s, b, impl->tb.count, why);
             else if (s.kind == Step::PACK) ok = check_pack(s, b, impl->tb.count, why);
+            else if (s.kind == Step::TC) ok = check_tc(s, b, impl->tb.count, why);
             else if (s.kind == Step::COPY)
                 ok = (s.copy_bytes <= b.bytes[s.src] && s.copy_bytes <= b.bytes[s.dst]) || fail(why, "copy size");
             if (!ok) {

@@ -117,6 +117,25 @@ int64_t TwiddleBuilder::add_linear(int64_t n, int64_t M, int64_t mult)
     return off;
 }
 
+int64_t TwiddleBuilder::add_dft_matrix(int R, int prec)
+{
+    for (const TwSeg& t : segs)
+        if (t.kind == 3 && t.M == R && t.R_or_mult == prec) return t.offset;
+    const int64_t n = gfft_tc_bmat_entries(R, prec);
+    if (n <= 0) return -1;
+    const int64_t off = count;
+    TwSeg s{};
+    s.offset = off;
+    s.count = n;
+    s.M = R;
+    s.R_or_mult = prec;
+    s.kind = 3;
+    segs.push_back(s);
+    count += n;
+    count += count & 1;
+    return off;
+}
+
 bool build_inner(int L, const std::vector<int>& radices, int nthr, TwiddleBuilder& tb, InnerPlan& ip)
 {
     if (radices.empty() || (int)radices.size() > kMaxPass) return false;
@@ -563,6 +582,91 @@ bool build_scratch_c2c_steps(int64_t n, int64_t batch, TwiddleBuilder& tb, std::
     return true;
 }
 
+namespace {
+
+// One tensor-core pass over sequences q = b*S + s of length L = R*R.
+Step tc_step(int L, int prec, int64_t nseq, int64_t S, int64_t in_dist, int64_t in_s, int64_t in_n,
+             int64_t out_dist, int64_t out_s, int64_t out_n, int64_t outer_n, TwiddleBuilder& tb)
+{
+    const int R = L == 256 ? 16 : 8;
+    const int TS = 128 / R;
+    Step st;
+    st.kind = Step::TC;
+    TcArgs& a = st.tc;
+    a.R = R;
+    a.prec = prec;
+    a.nseq = nseq;
+    a.S = S;
+    a.in_dist = in_dist;
+    a.in_s = in_s;
+    a.in_n = in_n;
+    a.out_dist = out_dist;
+    a.out_s = out_s;
+    a.out_n = out_n;
+    a.scale = 1.0f;
+    auto mode = [&](int64_t dist, int64_t ss, int64_t sn) {
+        // interleaved: side-by-side sequences, whole 16-byte pairs per tile
+        if (ss == 1 && S % TS == 0 && nseq % TS == 0 && dist % 2 == 0 && sn % 2 == 0) return (int)TC_IO_INTERLEAVED;
+        if (sn == 1 && ss % 2 == 0 && dist % 2 == 0) return (int)TC_IO_CONTIG;
+        return (int)TC_IO_GENERIC;
+    };
+    a.in_mode = mode(in_dist, in_s, in_n);
+    a.out_mode = mode(out_dist, out_s, out_n);
+    st.bmat_off = tb.add_dft_matrix(R, prec);
+    st.tw_off = tb.add_linear(L, L, 1);
+    if (outer_n > 1) {
+        // W_N^e = hi[e >> sh] * lo[e & mask], e < N
+        int sh = 0;
+        while ((int64_t(1) << (2 * sh)) < outer_n) ++sh;
+        a.otw_shift = sh;
+        a.otw_lo_n = 1 << sh;
+        a.otw_hi_n = (int)(((outer_n - 1) >> sh) + 1);
+        st.hi_off = tb.add_linear(a.otw_hi_n, outer_n, int64_t(1) << sh);
+        st.lo_off = tb.add_linear(a.otw_lo_n, outer_n, 1);
+    }
+    return st;
+}
+
+}  // namespace
+
+bool build_tc_c2c_steps(int64_t n, int64_t batch, int prec, bool inplace, TwiddleBuilder& tb, std::vector<Step>& out,
+                        int64_t& ws_bytes)
+{
+    if (prec != TC_PREC_TF32X3 && prec != TC_PREC_BF16X3) return false;
+    if (batch < 1) return false;
+    const int IN = inplace ? BUF_OUT : BUF_IN;
+    ws_bytes = 0;
+    out.clear();
+    if (n == 64 || n == 256) {
+        // one pass: sequence b contiguous; S = batch so every tile is one batch item
+        Step st = tc_step((int)n, prec, batch, batch, 0, n, 1, 0, n, 1, 1, tb);
+        st.src = IN;
+        st.dst = BUF_OUT;
+        out.push_back(st);
+        return true;
+    }
+    int64_t L1 = 0;
+    for (int64_t c : {int64_t(256), int64_t(64)})
+        if (n % c == 0 && (n / c == 64 || n / c == 256)) {
+            L1 = c;
+            break;
+        }
+    if (!L1) return false;
+    const int64_t L2 = n / L1;  // = S of the first pass
+    // pass 1: x[b*n + s + L2*n1] -> W_n^{s*k1} * X1 at ws[b*n + s + L2*k1]
+    Step p1 = tc_step((int)L1, prec, batch * L2, L2, n, 1, L2, n, 1, L2, n, tb);
+    p1.src = IN;
+    p1.dst = BUF_WS;
+    // pass 2: ws[b*n + k1*L2 + n2] -> out[b*n + k1 + L1*k2]
+    Step p2 = tc_step((int)L2, prec, batch * L1, L1, n, L2, 1, n, 1, L1, 1, tb);
+    p2.src = BUF_WS;
+    p2.dst = BUF_OUT;
+    out.push_back(p1);
+    out.push_back(p2);
+    ws_bytes = n * batch * 8;
+    return true;
+}
+
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
                  int64_t& ws2_bytes)
 {
@@ -606,6 +710,15 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
     if (!length_supported(N)) return unsupported("length has a prime factor > 47");
 
     if (p.kind == Kind::C2C) {
+        if (p.prec != 0 && p.stride == 1) {
+            int64_t ws = 0;
+            std::vector<Step> tc;
+            if (build_tc_c2c_steps(N, p.batch, p.prec, inplace, tb, tc, ws)) {
+                out.steps = tc;
+                need_ws(ws);
+                return true;
+            }
+        }
         bool spare = false;
         if (p.stride > 1) {
             // VERTICAL: transforms down the columns of [N][stride]

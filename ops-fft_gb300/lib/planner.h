@@ -38,16 +38,18 @@ std::vector<int> split_axis(int64_t n, int cap);
 enum BufId : int { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_WS2 = 3 };
 
 struct Step {
-    enum Kind { ROW, COL, PACK, COPY } kind = ROW;
+    enum Kind { ROW, COL, PACK, COPY, TC } kind = ROW;
     int64_t copy_bytes = 0;
     RowArgs row{};
     ColArgs col{};
     PackArgs pack{};
+    TcArgs tc{};
     int src = BUF_IN;
     int dst = BUF_OUT;
     // Offsets (float2 units) into the plan's twiddle blob for the pointers
     // patched at exec time; -1 when unused.
     int64_t tw_off = -1, post_off = -1, hi_off = -1, lo_off = -1;
+    int64_t bmat_off = -1;  // TC: DFT-matrix operand images
 };
 
 // Everything needed to run one transform kind (forward / adjoint variants
@@ -63,6 +65,7 @@ struct TwiddleBuilder {
     int64_t count = 0;  // float2 entries so far (kept 2-aligned)
     int64_t add_pass_table(int64_t ns, int R);        // rows of R, W_{ns*R}^{k*r}
     int64_t add_linear(int64_t count, int64_t M, int64_t mult);  // W_M^{i*mult}
+    int64_t add_dft_matrix(int R, int prec);  // tensor-core operand images (kind 3)
 };
 
 // Fill ip for length L with the given radices; register tables in tb.
@@ -81,6 +84,7 @@ struct Problem {
     int64_t batch = 1;
     int64_t stride = 1;      // VERTICAL 1D: stride between samples (= batch), batch = 1
     int weight = WEIGHT_NONE;
+    int prec = 0;            // 0: FP32 Stockham; TcPrec: split-precision tensor-core stages (C2C)
 };
 
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
@@ -90,6 +94,11 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
 // writes its whole output to BUF_WS, the second reads BUF_WS and writes
 // BUF_OUT.  False when n does not split into exactly two on-chip factors.
 bool build_scratch_c2c_steps(int64_t n, int64_t batch, TwiddleBuilder& tb, std::vector<Step>& out);
+
+// Split-precision tensor-core steps of a 1D batched C2C of length n
+// (64, 256 or a product of two of them).  False when n has no such split.
+bool build_tc_c2c_steps(int64_t n, int64_t batch, int prec, bool inplace, TwiddleBuilder& tb,
+                        std::vector<Step>& out, int64_t& ws_bytes);
 
 // Which transform length families are executable (reference domain).
 bool length_supported(int64_t n);

@@ -271,3 +271,103 @@ def test_vertical_and_2d_launches_stay_in_bounds():
         with A.Plan.plan2d(2, nx, ny, A.C2C) as p:
             if p.info().supported:
                 p.check()
+
+
+def test_precision_mode_extension():
+    """aclfftSetPrecisionMode: validation, re-plan of a made plan, which
+    lengths get tensor-core launches, and their launch bounds (no GPU)."""
+    assert A.lib().aclfftSetPrecisionMode(None, 1) == A.INVALID_PLAN
+    p = A.Plan.plan1d(4096, A.C2C, 256)
+    assert p.precision() == A.PREC_FP32 and p.info().tc_stages == 0
+    assert A.lib().aclfftSetPrecisionMode(p.handle, 3) == A.INVALID_VALUE
+    assert A.lib().aclfftSetPrecisionMode(p.handle, -1) == A.INVALID_VALUE
+    p.set_precision(A.PREC_TF32X3)
+    assert p.precision() == A.PREC_TF32X3 and p.info().tc_stages == 2
+    p.set_precision(A.PREC_FP32)
+    assert p.info().tc_stages == 0
+    p.destroy()
+    # set before MakePlan
+    h = ctypes.c_void_p()
+    assert A.lib().aclfftCreate(ctypes.byref(h)) == 0
+    assert A.lib().aclfftSetPrecisionMode(h, A.PREC_BF16X3) == 0
+    ws = ctypes.c_size_t()
+    assert A.lib().aclfftMakePlan1d(h, 65536, A.C2C, 64, 0, ctypes.byref(ws)) == 0
+    assert ws.value == 65536 * 64 * 8
+    A.lib().aclfftDestroy(h)
+    expect = {64: 1, 256: 1, 4096: 2, 16384: 2, 65536: 2, 1024: 0, 512: 0, 3000: 0, 128: 0, 1 << 20: 0}
+    for prec in (A.PREC_TF32X3, A.PREC_BF16X3):
+        for n, tc in expect.items():
+            for b in (1, 3, 13, 64):
+                with A.Plan.plan1d(n, A.C2C, b) as q:
+                    q.set_precision(prec)
+                    assert q.info().tc_stages == tc, (n, b, prec)
+                    assert q.check() == "ok"
+    # R2C/C2R, VERTICAL and 2D plans keep the FP32 kernels
+    for args in ((4096, A.R2C, 4, 0), (4096, A.C2R, 4, 0), (4096, A.C2C, 4, A.VERTICAL)):
+        with A.Plan.plan1d(*args) as q:
+            q.set_precision(A.PREC_TF32X3)
+            assert q.info().tc_stages == 0
+    with A.Plan.plan2d(2, 256, 256, A.C2C) as q:
+        q.set_precision(A.PREC_TF32X3)
+        assert q.info().tc_stages == 0
+
+
+def test_tc_index_maps_match_numpy_emulation():
+    """The tensor-core pass's row maps (stage A rows (n_a, t), stage B rows
+    (k_b, t)), its real-embedded DFT matrix and the two-pass 4-step split,
+    restated in numpy at FP64 and compared with the FP64 oracle."""
+    def bmat(R):
+        K = 2 * R
+        j = np.arange(R)
+        ang = 2 * np.pi * ((np.outer(j, j)) % R) / R
+        c, s = np.cos(ang), np.sin(ang)
+        B = np.zeros((K, K))
+        B[:R, :R], B[:R, R:], B[R:, :R], B[R:, R:] = c, s, -s, c   # rows: output re/im; cols: input re/im
+        return B
+
+    def tc_pass(inp, L, nseq, S, ind, ins, inn, outd, outs, outn, outer, out):
+        R = int(round(L ** 0.5))
+        TS = 128 // R
+        B = bmat(R)
+        twl = np.exp(-2j * np.pi * np.arange(L) / L)
+        m = np.arange(128)
+        ra, rt = m // TS, m % TS
+        for q0 in range(0, nseq, TS):
+            nv = min(TS, nseq - q0)
+            bb, s0 = q0 // S, q0 % S
+            stg = np.zeros((TS, L), complex)
+            for t in range(nv):
+                stg[t] = inp[bb * ind + (s0 + t) * ins + np.arange(L) * inn]
+            x = stg[rt[:, None], ra[:, None] + R * np.arange(R)[None, :]]
+            D = np.concatenate([x.real, x.imag], 1) @ B.T
+            y = (D[:, :R] + 1j * D[:, R:]) * twl[ra[:, None] * np.arange(R)[None, :]]
+            A2 = np.zeros((128, 2 * R))
+            rows = np.arange(R)[None, :] * TS + rt[:, None]
+            A2[rows, ra[:, None]] = y.real
+            A2[rows, R + ra[:, None]] = y.imag
+            D2 = A2 @ B.T
+            z = D2[:, :R] + 1j * D2[:, R:]
+            for mm in range(128):
+                kb, t = mm // TS, mm % TS
+                if t >= nv:
+                    continue
+                s = (q0 + t) % S
+                k = kb + R * np.arange(R)
+                v = z[mm]
+                if outer > 1:
+                    v = v * np.exp(-2j * np.pi * ((s * k) % outer) / outer)
+                out[bb * outd + s * outs + k * outn] = v
+
+    rng = np.random.default_rng(4)
+    for n, b in ((64, 19), (256, 13), (4096, 2)):
+        x = rng.standard_normal(n * b) + 1j * rng.standard_normal(n * b)
+        out = np.zeros(n * b, complex)
+        if n <= 256:
+            tc_pass(x, n, b, b, 0, n, 1, 0, n, 1, 1, out)
+        else:
+            L1, L2 = 64, 64
+            ws = np.zeros(n * b, complex)
+            tc_pass(x, L1, b * L2, L2, n, 1, L2, n, 1, L2, n, ws)
+            tc_pass(ws, L2, b * L1, L1, n, L2, 1, n, 1, L1, 1, out)
+        e = O.errors(out, O.c2c(x.reshape(b, n), -1))
+        assert e["rel_l2"] < 1e-13, (n, b, e)
