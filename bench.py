@@ -211,12 +211,18 @@ class Cfg2:
 
 
 class C2CWorkload:
-    """Plain batched C2C (cfg1: 4096 x 256; cfg3: 65536 x 64 and 16384 x 64)."""
+    """Plain batched C2C (cfg1: 4096 x 256; cfg3: 65536 x 64 and 16384 x 64).
 
-    def __init__(self, torch, A, dev, stream, nsets, sizes, name, uniform):
+    ``prec`` selects the DFT-stage arithmetic (aclfftSetPrecisionMode): the
+    FP32 Stockham kernels or the split-precision tensor-core forms."""
+
+    FORM_NAMES = {0: "fp32 stockham", 1: "tf32x3 tensor-core", 2: "bf16x3 tensor-core"}
+
+    def __init__(self, torch, A, dev, stream, nsets, sizes, name, uniform, prec=0):
         self.torch, self.A = torch, A
         self.sizes = sizes
         self.name = name
+        self.stream = stream
         g = torch.Generator(device="cpu").manual_seed(12345)
         self.plans = {}
         self.sets = []
@@ -224,6 +230,7 @@ class C2CWorkload:
             p = A.Plan.plan1d(n, A.C2C, b)
             p.set_stream(stream)
             self.plans[n] = p
+        self.set_prec(prec)
         for _ in range(nsets):
             s = {}
             for n, b in sizes:
@@ -235,11 +242,37 @@ class C2CWorkload:
             self.sets.append(s)
         self.bytes_per_transform = {n: 16 * n * b for n, b in sizes}
         self.alg_bytes_per_step = sum(self.bytes_per_transform.values())
-        self.launches_per_step = sum(len([1]) * self.plans[n].info().nsteps for n, _ in sizes)
-        n0 = sizes[0][0]
-        self.dominant = (f"C2C N={n0} batch={sizes[0][1]}", self.bytes_per_transform[n0])
-        self.dom_n = n0
+        self.dom_n = sizes[0][0]
         self.set_bytes = sum(16 * n * b for n, b in sizes)
+        self._describe()
+
+    def set_prec(self, prec):
+        self.prec = prec
+        for p in self.plans.values():
+            p.set_precision(prec)
+            p.set_stream(self.stream)
+        if hasattr(self, "bytes_per_transform"):
+            self._describe()
+
+    def _describe(self):
+        self.launches_per_step = sum(self.plans[n].info().nsteps for n, _ in self.sizes)
+        n0, b0 = self.sizes[0]
+        self.dominant = (f"C2C N={n0} batch={b0} ({self.FORM_NAMES[self.prec]})", self.bytes_per_transform[n0])
+
+    def fp64_errors(self):
+        """rel-L2 / max-abs of this form against torch's complex128 FFT of the
+        same (first) input set, per length."""
+        torch = self.torch
+        out = {}
+        s = self.sets[0]
+        for n, _ in self.sizes:
+            self.plans[n].exec_c2c(s[n]["x"], s[n]["y"], self.A.FORWARD)
+            torch.cuda.synchronize()
+            ref = torch.fft.fft(s[n]["x"].to(torch.complex128), dim=-1)
+            d = s[n]["y"].to(torch.complex128) - ref
+            out[str(n)] = {"rel_l2": float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(ref)),
+                           "max_abs": float(d.abs().max())}
+        return out
 
     def step(self, i, dom_events=None):
         s = self.sets[i % len(self.sets)]
@@ -289,7 +322,8 @@ def make_workload(name, torch, A, dev, stream, nsets):
         return C2CWorkload(torch, A, dev, stream, nsets, [(4096, 256)], "1D C2C forward N=4096 batch=256", True)
     if name == "cfg3":
         return C2CWorkload(torch, A, dev, stream, nsets, [(65536, 64), (16384, 64)],
-                           "1D C2C forward N=65536,16384 batch=64 (FP32 Stockham form)", False)
+                           "1D C2C forward N=65536,16384 batch=64 (split-precision TF32x3 tensor-core form)", False,
+                           prec=A.PREC_TF32X3)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -355,28 +389,44 @@ def main():
     torch.cuda.empty_cache()
     wl = make_workload(args.workload, torch, A, dev, stream, nsets)
 
-    for i in range(args.warmup):
-        wl.step(i)
-    torch.cuda.synchronize()
+    def timed(nk):
+        for i in range(args.warmup):
+            wl.step(i)
+        torch.cuda.synchronize()
+        dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0.record()
+        for i in range(nk):
+            wl.step(i, dom_ev[i])
+        t1.record()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        return t0.elapsed_time(t1), statistics.mean(a.elapsed_time(b) for a, b in dom_ev)
 
     nk = args.steps
-    dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
-    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    forms = None
+    if isinstance(wl, C2CWorkload):
+        # every arithmetic form of the same workload, for comparison; the
+        # headline line is then timed in the workload's own form
+        forms = {}
+        own = wl.prec
+        for prec in (A.PREC_FP32, A.PREC_BF16X3, A.PREC_TF32X3):
+            wl.set_prec(prec)
+            f_ms, f_dom = timed(nk)
+            forms[wl.FORM_NAMES[prec]] = {
+                "GB/s": round(wl.alg_bytes_per_step * nk / (f_ms / 1e3) / 1e9, 1),
+                "dominant_us": round(f_dom * 1e3, 2), "launches_per_step": wl.launches_per_step,
+                "fp64_error": wl.fp64_errors()}
+        wl.set_prec(own)
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     time.sleep(0.3)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t0.record()
-    for i in range(nk):
-        wl.step(i, dom_ev[i])
-    t1.record()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    ms, dom_ms = timed(nk)
     clk = clocks.stop()
-    ms = t0.elapsed_time(t1)
     if dist:
         tt = torch.tensor([ms], device=dev)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -384,7 +434,6 @@ def main():
     ms_per_step = ms / nk
     value = wl.alg_bytes_per_step * world * nk / (ms / 1e3) / 1e9
 
-    dom_ms = statistics.mean(a.elapsed_time(b) for a, b in dom_ev)
     peak, peak_kind = _peaks()
     achieved = wl.dominant[1] / (dom_ms / 1e3) / 1e9
     traffic = NCU_TRAFFIC.get((args.workload, "dominant"))
@@ -423,6 +472,9 @@ def main():
         cfg = wl.config()
         cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
+        if forms is not None:
+            cfg["forms"] = forms
+            cfg["fp64_reference"] = "torch.fft.fft in complex128 on the same device inputs"
         line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": nk,
                 "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
