@@ -2,7 +2,7 @@
 """Benchmark of the batched FP32 transform path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|cfg4]
+                    [--workload cfg2|cfg1|cfg3|cfg5]
 
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
@@ -315,6 +315,112 @@ class C2CWorkload:
         return {"workload": self.name, "sizes": [list(s) for s in self.sizes], "dtype": "complex64 interleaved"}
 
 
+class Cfg5:
+    """Ragged batch: 10000 1D transforms, lengths log-uniform over the 7-smooth
+    integers in [16, 32768], 70% C2C / 30% R2C, x ~ N(0,1), one persistent
+    launch per step (replayed CUDA graph, autotuned per-length plans)."""
+
+    def __init__(self, torch, A, dev, stream, nsets):
+        import numpy as np
+
+        self.torch, self.A = torch, A
+        self.lengths, self.types = A.ragged_lengths(10000, seed=12345)
+        self.ino, self.outo, ci, co = A.ragged_layout(self.lengths, self.types)
+        self.plan = A.RaggedPlan(self.lengths, self.types, self.ino, self.outo)
+        self.plan.set_stream(stream)
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        self.sets = []
+        for _ in range(nsets):
+            self.sets.append(dict(x=torch.randn(ci // 4, generator=g).to(dev),
+                                  y=torch.zeros(co // 4, dtype=torch.float32, device=dev)))
+        n = self.lengths.astype(np.int64)
+        c2c = self.types == A.C2C
+        self.alg_bytes_per_step = int(np.sum(np.where(c2c, 16 * n, 4 * n + 8 * (n // 2 + 1))))
+        self.launches_per_step = 1
+        self.dominant = ("ragged persistent launch (10000 transforms)", self.alg_bytes_per_step)
+        self.set_bytes = ci + co
+        self.in_bytes, self.out_bytes = ci, co
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        if dom_events is not None:
+            dom_events[0].record()
+        self.plan.exec(s["x"], s["y"], self.A.FORWARD)
+        if dom_events is not None:
+            dom_events[1].record()
+
+    def make_host(self):
+        torch = self.torch
+        self.hx = torch.empty(self.in_bytes // 4, dtype=torch.float32, pin_memory=True)
+        self.hx.copy_(self.sets[0]["x"].cpu())
+        self.hy = torch.empty(self.out_bytes // 4, dtype=torch.float32, pin_memory=True)
+        return self.in_bytes, self.out_bytes
+
+    def step_host(self):
+        # the ragged entry point takes device pointers: the host path is the
+        # copy in, the exec and the copy out, all on the plan's stream
+        s = self.sets[0]
+        s["x"].copy_(self.hx, non_blocking=True)
+        self.plan.exec(s["x"], s["y"], self.A.FORWARD)
+        self.hy.copy_(s["y"], non_blocking=True)
+
+    def fp64_errors(self, sample=300):
+        """Per-transform rel-L2 against torch's complex128 FFT for the first
+        `sample` transforms: worst and median."""
+        import numpy as np
+
+        torch = self.torch
+        s = self.sets[0]
+        self.plan.exec(s["x"], s["y"], self.A.FORWARD)
+        torch.cuda.synchronize()
+        errs = []
+        for n, t, io, oo in list(zip(self.lengths, self.types, self.ino, self.outo))[:sample]:
+            n = int(n)
+            if t == self.A.C2C:
+                x = s["x"][io // 4: io // 4 + 2 * n].view(torch.complex64).to(torch.complex128)
+                ref = torch.fft.fft(x)
+                y = s["y"][oo // 4: oo // 4 + 2 * n].view(torch.complex64).to(torch.complex128)
+            else:
+                x = s["x"][io // 4: io // 4 + n].to(torch.float64)
+                ref = torch.fft.rfft(x)
+                y = s["y"][oo // 4: oo // 4 + 2 * (n // 2 + 1)].view(torch.complex64).to(torch.complex128)
+            errs.append(float(torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref)))
+        return {"transforms_checked": len(errs), "worst_rel_l2": max(errs), "median_rel_l2": float(np.median(errs))}
+
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        done = 0
+        t0 = time.perf_counter()
+        k = 0
+        budget = rows * 4096 * 16  # bytes of transforms to sample
+        for n, t in zip(self.lengths, self.types):
+            n = int(n)
+            if t == self.A.C2C:
+                x = (rng.standard_normal((1, n)) + 1j * rng.standard_normal((1, n))).astype(np.complex64)
+                O.port_c2c(x, -1, nthreads)
+                done += 16 * n
+            else:
+                x = rng.standard_normal((1, n)).astype(np.float32)
+                O.port_r2c(x, nthreads)
+                done += 4 * n + 8 * (n // 2 + 1)
+            k += 1
+            if done >= budget:
+                break
+        self.cpu_transforms = k
+        return done, time.perf_counter() - t0
+
+    def config(self):
+        inf = self.plan.info()
+        return {"workload": "ragged batch: 10000 1D transforms in one persistent launch",
+                "lengths": "log-uniform over 2^a 3^b 5^c 7^d in [16, 32768] (seed 12345)",
+                "kinds": "70% C2C / 30% R2C", "classes": inf.classes, "long_transforms": inf.long_transforms,
+                "work_items": inf.items, "tuned_classes": inf.tuned_classes, "cuda_graph": bool(inf.graph),
+                "device_resident_bytes": int(self.set_bytes * len(self.sets) + inf.workspace_bytes +
+                                             inf.twiddle_entries * 8)}
+
+
 def make_workload(name, torch, A, dev, stream, nsets):
     if name == "cfg2":
         return Cfg2(torch, A, dev, stream, nsets)
@@ -324,6 +430,8 @@ def make_workload(name, torch, A, dev, stream, nsets):
         return C2CWorkload(torch, A, dev, stream, nsets, [(65536, 64), (16384, 64)],
                            "1D C2C forward N=65536,16384 batch=64 (split-precision TF32x3 tensor-core form)", False,
                            prec=A.PREC_TF32X3)
+    if name == "cfg5":
+        return Cfg5(torch, A, dev, stream, nsets)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -472,6 +580,8 @@ def main():
         cfg = wl.config()
         cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
+        if isinstance(wl, Cfg5):
+            cfg["fp64_error"] = wl.fp64_errors()
         if forms is not None:
             cfg["forms"] = forms
             cfg["fp64_reference"] = "torch.fft.fft in complex128 on the same device inputs"

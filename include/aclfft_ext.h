@@ -104,6 +104,56 @@ ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host
 ACLFFT_API aclfftResult aclfftExecC2CNoAlloc(const aclfftComplex* idata, aclfftComplex* odata, int nx, int batch,
                                              int direction, cudaStream_t stream);
 
+/* Ragged batches (no counterpart in the reference, which runs one exec per
+ * (length, kind) plan): `count` 1D transforms of different lengths and kinds
+ * executed by ONE persistent kernel launch driven by a device work-descriptor
+ * table.  Transform i is C2C or R2C (types[i]) of length lengths[i] (2 ..
+ * 2^24, prime factors <= 13); its input starts inOffsets[i] bytes and its
+ * output outOffsets[i] bytes after the pointers given to aclfftRaggedExec
+ * (both offsets multiples of 8; C2C: n complex in and out; R2C: n reals in,
+ * n/2 + 1 complex out).  Lengths above 4096 (complex) run as two dependent
+ * steps inside the same launch using a plan-owned workspace.  Per (kind,
+ * length) the radix order and threads per transform come from an autotuner
+ * (timed candidates, cached per process and in the file named by
+ * OPS_FFT_TUNE_CACHE) that runs on the first exec unless disabled.  Execs
+ * replay a CUDA graph captured per (input, output, direction); inside a
+ * caller's stream capture they are recorded into that capture instead.
+ * Unnormalised; direction applies to the C2C transforms (R2C transforms are
+ * always forward). */
+typedef struct aclfftRaggedPlan_t* aclfftRaggedPlan;
+
+typedef struct aclfftRaggedInfo_t {
+    int transforms;
+    int classes;          /* distinct (kind, length) */
+    int long_transforms;  /* transforms run as two dependent steps */
+    int items;            /* work items per exec */
+    int tuned_classes;    /* classes whose plan came from the autotuner */
+    int graph;            /* 1 when execs replay a captured CUDA graph */
+    int smem_bytes;       /* shared memory per CTA */
+    long long twiddle_entries;
+    size_t workspace_bytes;
+    size_t in_bytes_min;  /* input extent implied by the offsets */
+    size_t out_bytes_min; /* output extent implied by the offsets */
+} aclfftRaggedInfo;
+
+ACLFFT_API aclfftResult aclfftRaggedPlanCreate(aclfftRaggedPlan* plan, int count, const int* lengths,
+                                               const aclfftType* types, const long long* inOffsets,
+                                               const long long* outOffsets);
+ACLFFT_API aclfftResult aclfftRaggedSetStream(aclfftRaggedPlan plan, cudaStream_t stream);
+/* autotune: tune on the first exec (default 1); useGraph: replay a captured
+ * CUDA graph (default 1). */
+ACLFFT_API aclfftResult aclfftRaggedSetOptions(aclfftRaggedPlan plan, int autotune, int useGraph);
+ACLFFT_API aclfftResult aclfftRaggedAutotune(aclfftRaggedPlan plan);
+/* idata/odata: device pointers; asynchronous on the plan's stream. */
+ACLFFT_API aclfftResult aclfftRaggedExec(aclfftRaggedPlan plan, void* idata, void* odata, int direction);
+ACLFFT_API aclfftResult aclfftRaggedGetInfo(aclfftRaggedPlan plan, aclfftRaggedInfo* info);
+/* Device error flags of the plan's launches (bit 2: a dependency wait ran
+ * out of time); synchronises with the device. */
+ACLFFT_API aclfftResult aclfftRaggedGetError(aclfftRaggedPlan plan, int* flags);
+ACLFFT_API aclfftResult aclfftRaggedDestroy(aclfftRaggedPlan plan);
+/* Host replay of every work item's index ranges (0 = all in bounds). */
+ACLFFT_API int aclfftRaggedDebugCheck(aclfftRaggedPlan plan, char* msg, int msglen);
+
 /* Replays the address arithmetic of every launch the plan can make against
  * the buffer sizes of each call variant (no kernel runs).  Returns 0 when
  * all launches stay in bounds; msg receives a description. */

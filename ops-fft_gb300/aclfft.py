@@ -85,6 +85,22 @@ class AclfftError(RuntimeError):
 
 _lib = None
 
+class RaggedInfo(ctypes.Structure):
+    _fields_ = [
+        ("transforms", ctypes.c_int),
+        ("classes", ctypes.c_int),
+        ("long_transforms", ctypes.c_int),
+        ("items", ctypes.c_int),
+        ("tuned_classes", ctypes.c_int),
+        ("graph", ctypes.c_int),
+        ("smem_bytes", ctypes.c_int),
+        ("twiddle_entries", ctypes.c_longlong),
+        ("workspace_bytes", ctypes.c_size_t),
+        ("in_bytes_min", ctypes.c_size_t),
+        ("out_bytes_min", ctypes.c_size_t),
+    ]
+
+
 _H = ctypes.c_void_p
 _HP = ctypes.POINTER(ctypes.c_void_p)
 _I = ctypes.c_int
@@ -127,6 +143,15 @@ _SIGNATURES = {
     "aclfftGetTwiddles": [_H, _VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
     "aclfftDebugCheckPlan": [_H, ctypes.c_char_p, _I],
     "aclfftExecC2CNoAlloc": [_VP, _VP, _I, _I, _I, _VP],
+    "aclfftRaggedPlanCreate": [_HP, _I, _VP, _VP, _VP, _VP],
+    "aclfftRaggedSetStream": [_H, _VP],
+    "aclfftRaggedSetOptions": [_H, _I, _I],
+    "aclfftRaggedAutotune": [_H],
+    "aclfftRaggedExec": [_H, _VP, _VP, _I],
+    "aclfftRaggedGetInfo": [_H, ctypes.POINTER(RaggedInfo)],
+    "aclfftRaggedGetError": [_H, ctypes.POINTER(_I)],
+    "aclfftRaggedDestroy": [_H],
+    "aclfftRaggedDebugCheck": [_H, ctypes.c_char_p, _I],
 }
 
 
@@ -268,3 +293,118 @@ class Plan:
 
     def __exit__(self, *exc):
         self.destroy()
+
+
+class RaggedPlan:
+    """Owning wrapper of an aclfftRaggedPlan: many 1D C2C / R2C transforms of
+    different lengths executed by one persistent launch.
+
+    lengths, types (C2C or R2C per transform) and byte offsets of each
+    transform's input and output relative to the exec pointers."""
+
+    def __init__(self, lengths, types, in_offsets, out_offsets):
+        import numpy as np
+
+        n = len(lengths)
+        self._len = np.ascontiguousarray(lengths, dtype=np.int32)
+        self._typ = np.ascontiguousarray(types, dtype=np.int32)
+        self._ino = np.ascontiguousarray(in_offsets, dtype=np.int64)
+        self._outo = np.ascontiguousarray(out_offsets, dtype=np.int64)
+        self.handle = ctypes.c_void_p()
+        _check(lib().aclfftRaggedPlanCreate(ctypes.byref(self.handle), n, self._len.ctypes.data,
+                                            self._typ.ctypes.data, self._ino.ctypes.data, self._outo.ctypes.data),
+               "aclfftRaggedPlanCreate")
+
+    def set_stream(self, stream) -> None:
+        s = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        _check(lib().aclfftRaggedSetStream(self.handle, s), "aclfftRaggedSetStream")
+
+    def set_options(self, autotune: bool = True, graph: bool = True) -> None:
+        _check(lib().aclfftRaggedSetOptions(self.handle, int(autotune), int(graph)), "aclfftRaggedSetOptions")
+
+    def autotune(self) -> None:
+        _check(lib().aclfftRaggedAutotune(self.handle), "aclfftRaggedAutotune")
+
+    def exec(self, x, y, direction: int = FORWARD) -> None:
+        _check(lib().aclfftRaggedExec(self.handle, ptr(x), ptr(y), direction), "aclfftRaggedExec")
+
+    def info(self) -> RaggedInfo:
+        inf = RaggedInfo()
+        _check(lib().aclfftRaggedGetInfo(self.handle, ctypes.byref(inf)), "aclfftRaggedGetInfo")
+        return inf
+
+    def error_flags(self) -> int:
+        f = _I()
+        _check(lib().aclfftRaggedGetError(self.handle, ctypes.byref(f)), "aclfftRaggedGetError")
+        return f.value
+
+    def check(self) -> str:
+        buf = ctypes.create_string_buffer(256)
+        rc = lib().aclfftRaggedDebugCheck(self.handle, buf, 256)
+        msg = buf.value.decode()
+        if rc != 0:
+            raise AssertionError(msg)
+        return msg
+
+    def destroy(self) -> None:
+        if self.handle and self.handle.value:
+            lib().aclfftRaggedDestroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+
+def ragged_lengths(count: int, lo: int = 16, hi: int = 32768, c2c_frac: float = 0.7, seed: int = 12345,
+                   primes=(2, 3, 5, 7)):
+    """Seeded ragged workload: lengths log-uniform over the integers in
+    [lo, hi] whose prime factors are in `primes` (a log-uniform draw snapped
+    to the nearest such length), kinds C2C with probability c2c_frac else
+    R2C.  Returns (lengths, types) as numpy int arrays."""
+    import numpy as np
+
+    smooth = [1]
+    for p in primes:
+        nxt = []
+        for v in smooth:
+            x = v
+            while x <= hi:
+                nxt.append(x)
+                x *= p
+        smooth = sorted(set(nxt))
+    smooth = np.array([v for v in smooth if lo <= v <= hi], dtype=np.int64)
+    logs = np.log(smooth.astype(np.float64))
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(np.log(lo), np.log(hi), size=count)
+    idx = np.clip(np.searchsorted(logs, u), 1, len(smooth) - 1)
+    pick = np.where(np.abs(logs[idx - 1] - u) <= np.abs(logs[idx] - u), idx - 1, idx)
+    lengths = smooth[pick].astype(np.int32)
+    types = np.where(rng.uniform(size=count) < c2c_frac, C2C, R2C).astype(np.int32)
+    return lengths, types
+
+
+def ragged_layout(lengths, types, align: int = 256):
+    """Packed byte offsets of each transform's input and output (each start
+    rounded up to `align` bytes) and the total input / output bytes."""
+    import numpy as np
+
+    ino = np.zeros(len(lengths), dtype=np.int64)
+    outo = np.zeros(len(lengths), dtype=np.int64)
+    ci = co = 0
+    for i, (n, t) in enumerate(zip(lengths, types)):
+        n = int(n)
+        ino[i], outo[i] = ci, co
+        inb = 8 * n if t == C2C else 4 * n
+        outb = 8 * n if t == C2C else 8 * (n // 2 + 1)
+        ci += -(-inb // align) * align
+        co += -(-outb // align) * align
+    return ino, outo, ci, co

@@ -164,6 +164,73 @@ struct TcArgs {
     float scale;
 };
 
+// Ragged batches: many transforms of different lengths and kinds in one
+// persistent launch.  A transform class (one kind and length) owns an
+// on-chip plan; a work item is a group of same-class transforms done on chip
+// (RAG_SINGLE), or one step of a long transform split as n' = L1*L2 (n' = n
+// for C2C, n/2 for even R2C): RAG_P1 (a group of the L2 columns: length-L1
+// transforms of x[j + L2*i] into the workspace), RAG_P2 (a group of the L1
+// rows: twiddled length-L2 transforms from the workspace into the output,
+// or into the second workspace half for R2C) and RAG_POST (even/odd
+// post-process of a long R2C).  P2 items wait until all P1 items of their
+// transform are done, POST items until all P2 items are; items are queued in
+// that order, so every wait is on items already being processed.
+enum RagType : int32_t { RAG_C2C = 0, RAG_R2C = 1 };
+enum RagMode : int32_t { RAG_MODE_SINGLE = 0, RAG_MODE_LONG = 1 };
+enum RagItemKind : int32_t { RAG_SINGLE = 0, RAG_P1 = 1, RAG_P2 = 2, RAG_POST = 3 };
+
+struct RagClass {
+    InnerPlan ip;      // single: the whole on-chip transform (length L); long: length L1
+    InnerPlan ip2;     // long: length L2
+    int32_t n;         // transform length
+    int32_t type;      // RagType
+    int32_t mode;      // RagMode
+    int32_t L;         // complex length transformed (n for C2C and odd R2C, n/2 for even R2C)
+    int32_t L1, L2;    // long: L = L1 * L2
+    int32_t group;     // single: transforms per item; long: columns per P1 item
+    int32_t group2;    // long: rows per P2 item
+    int32_t pitch;     // single: shared-memory pitch of one transform (float2)
+    int32_t otw_shift; // long: W_L^{k1*n2} = hi[e >> shift] * lo[e & mask]
+    int64_t post_off;  // even R2C: W_n^k, k <= n/4 + 1 (float2 offset in the blob)
+    int64_t hi_off, lo_off;
+};
+
+struct RagXform {
+    int64_t in_off;   // byte offsets from the exec's input / output pointers
+    int64_t out_off;
+    int64_t ws_off;   // long transforms: float2 offset of its workspace (2*L for R2C, L for C2C)
+    int32_t cls;
+    int32_t pad_;
+};
+
+struct RagItem {
+    int32_t kind;   // RagItemKind
+    int32_t cls;
+    int32_t first;  // single: index into the order array; P1/P2: first column / row
+    int32_t count;  // transforms / columns / rows in this item
+    int32_t xform;  // P1/P2/POST: the transform
+    int32_t need;   // P2/POST: completed items of the transform to wait for
+};
+
+struct RagArgs {
+    const RagClass* cls;
+    const RagXform* xf;
+    const int32_t* order;  // single items: transform indices grouped by class
+    const RagItem* items;
+    int32_t nitems;
+    int32_t smem_bytes;
+    int32_t ctas;   // persistent CTAs to launch (gfft_ragged_ctas * SM count)
+    int32_t pad_;
+    int* queue;     // queue[0]: next item; queue[1 + x]: completed items of transform x
+    int* err;
+    const void* tw;
+    const void* in;
+    void* out;
+    void* ws;  // float2 workspace
+    int32_t inverse;  // C2C transforms run backward (R2C transforms are always forward)
+    float scale_c2c;  // applied to C2C outputs
+};
+
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
 //   kind 1: f(i) = (i * mult) mod M               (linear tables)
 //   kind 2: f(i) = ((i / ns) * (i % ns)) mod M    (pass tables, [r][k] layout)
@@ -186,6 +253,11 @@ int gfft_launch_row(const gfft::RowArgs* a, void* stream);
 int gfft_launch_col(const gfft::ColArgs* a, void* stream);
 int gfft_launch_pack(const gfft::PackArgs* a, void* stream);
 int gfft_launch_tc(const gfft::TcArgs* a, void* stream);
+int gfft_launch_ragged(const gfft::RagArgs* a, void* stream);
+// Prepares the ragged kernel for a shared-memory size (attributes) and
+// returns its resident CTAs per SM (0 on error).  Not stream-ordered: call
+// outside stream capture.
+int gfft_ragged_ctas(int smem_bytes);
 // float2 entries of the two DFT-matrix operand images for (R, prec).
 long long gfft_tc_bmat_entries(int R, int prec);
 int gfft_tc_gen_bmat(void* dst, int R, int prec, void* stream);
