@@ -2,7 +2,7 @@
 """Benchmark of the batched FP32 transform path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|cfg5]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5]
 
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
@@ -315,6 +315,89 @@ class C2CWorkload:
         return {"workload": self.name, "sizes": [list(s) for s in self.sizes], "dtype": "complex64 interleaved"}
 
 
+class Cfg4:
+    """2D C2C 2048 x 2048, batch 8: forward, inverse normalised by 1/(2048^2),
+    and the backward pass of L = sum Re(conj(Y) * G) (the adjoint of the
+    forward transform applied to G)."""
+
+    def __init__(self, torch, A, dev, stream, nsets):
+        self.torch, self.A = torch, A
+        self.b, self.nx, self.ny = 8, 2048, 2048
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        shape = (self.b, self.nx, self.ny)
+        self.pf = A.Plan.plan2d(self.b, self.nx, self.ny, A.C2C)
+        self.pi = A.Plan.plan2d(self.b, self.nx, self.ny, A.C2C)
+        self.pi.set_norm(A.NORM_BACKWARD)
+        for p in (self.pf, self.pi):
+            p.set_stream(stream)
+        self.sets = []
+        for _ in range(nsets):
+            x = torch.complex(torch.rand(shape, generator=g) * 2 - 1, torch.rand(shape, generator=g) * 2 - 1)
+            G = torch.complex(torch.randn(shape, generator=g), torch.randn(shape, generator=g))
+            self.sets.append(dict(x=x.to(dev), G=G.to(dev), Y=torch.empty(shape, dtype=torch.complex64, device=dev),
+                                  Z=torch.empty(shape, dtype=torch.complex64, device=dev),
+                                  gx=torch.empty(shape, dtype=torch.complex64, device=dev)))
+        per = 16 * self.b * self.nx * self.ny
+        self.alg_bytes_per_step = 3 * per
+        self.launches_per_step = 3 * self.pf.info().nsteps
+        self.dominant = ("2D C2C 2048x2048 batch=8 forward (row + column pass)", per)
+        self.set_bytes = 5 * per // 2
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        if dom_events is not None:
+            dom_events[0].record()
+        self.pf.exec_c2c(s["x"], s["Y"], self.A.FORWARD)
+        if dom_events is not None:
+            dom_events[1].record()
+        self.pi.exec_c2c(s["Y"], s["Z"], self.A.BACKWARD)
+        self.pf.exec_c2c_adjoint(s["G"], s["gx"], self.A.FORWARD)
+
+    def make_host(self):
+        torch = self.torch
+        s = self.sets[0]
+        self.host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s.items()}
+        for k, v in s.items():
+            self.host[k].copy_(v.cpu())
+        per = 8 * self.b * self.nx * self.ny
+        return 3 * per, 3 * per
+
+    def step_host(self):
+        h = self.host
+        self.pf.exec_c2c(h["x"], h["Y"], self.A.FORWARD)
+        self.pi.exec_c2c(h["Y"], h["Z"], self.A.BACKWARD)
+        self.pf.exec_c2c_adjoint(h["G"], h["gx"], self.A.FORWARD)
+
+    def fp64_errors(self):
+        torch = self.torch
+        s = self.sets[0]
+        self.step(0)
+        torch.cuda.synchronize()
+        x = s["x"][0].to(torch.complex128)
+        ref = torch.fft.fft2(x)
+        y = s["Y"][0].to(torch.complex128)
+        rt = s["Z"].to(torch.complex128) - s["x"].to(torch.complex128)
+        return {"forward_image0_rel_l2": float(torch.linalg.vector_norm(y - ref) / torch.linalg.vector_norm(ref)),
+                "round_trip_rel_l2": float(torch.linalg.vector_norm(rt) / torch.linalg.vector_norm(s["x"]))}
+
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        m = max(1, min(8, rows // 64))
+        x = (rng.uniform(-1, 1, (m, self.nx, self.ny)) + 1j * rng.uniform(-1, 1, (m, self.nx, self.ny))).astype(
+            np.complex64)
+        t0 = time.perf_counter()
+        # the port transforms rows; a 2D transform is rows then columns
+        y = O.port_c2c(x.reshape(-1, self.ny), -1, nthreads).reshape(m, self.nx, self.ny)
+        O.port_c2c(np.ascontiguousarray(y.transpose(0, 2, 1)).reshape(-1, self.nx), -1, nthreads)
+        return 16 * m * self.nx * self.ny, time.perf_counter() - t0
+
+    def config(self):
+        return {"workload": "2D C2C 2048x2048 batch=8: forward, inverse (1/N^2), backward of sum Re(conj(Y) G)",
+                "dtype": "complex64 interleaved", "launches_per_transform": self.pf.info().nsteps}
+
+
 class Cfg5:
     """Ragged batch: 10000 1D transforms, lengths log-uniform over the 7-smooth
     integers in [16, 32768], 70% C2C / 30% R2C, x ~ N(0,1), one persistent
@@ -430,6 +513,8 @@ def make_workload(name, torch, A, dev, stream, nsets):
         return C2CWorkload(torch, A, dev, stream, nsets, [(65536, 64), (16384, 64)],
                            "1D C2C forward N=65536,16384 batch=64 (split-precision TF32x3 tensor-core form)", False,
                            prec=A.PREC_TF32X3)
+    if name == "cfg4":
+        return Cfg4(torch, A, dev, stream, nsets)
     if name == "cfg5":
         return Cfg5(torch, A, dev, stream, nsets)
     raise SystemExit(f"unknown workload {name}")
@@ -580,7 +665,7 @@ def main():
         cfg = wl.config()
         cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
-        if isinstance(wl, Cfg5):
+        if isinstance(wl, (Cfg4, Cfg5)):
             cfg["fp64_error"] = wl.fp64_errors()
         if forms is not None:
             cfg["forms"] = forms

@@ -345,6 +345,27 @@ def test_adjoint_c2c_against_fd():
         _fp64_ok(out.reshape(-1), gfd, bound=1e-5, what=("c2c adjoint", d))
 
 
+def test_adjoint_2d_against_fd_32x32():
+    """2D C2C backward pass through L = sum Re(conj(G) * F2(x)) on a 32x32
+    instance (and the normalised inverse), against FP64 central differences."""
+    nx = ny = 32
+    rng = np.random.default_rng(4)
+    x = rng.uniform(-1, 1, (nx, ny)) + 1j * rng.uniform(-1, 1, (nx, ny))
+    G = rng.standard_normal((nx, ny)) + 1j * rng.standard_normal((nx, ny))
+    for d, norm, scale in ((A.FORWARD, A.NORM_NONE, 1.0), (A.BACKWARD, A.NORM_BACKWARD, 1.0 / (nx * ny))):
+        def L(v):
+            z = (v[: v.size // 2] + 1j * v[v.size // 2:]).reshape(nx, ny)
+            return float(np.sum(np.real(np.conj(G) * O.c2c_2d(z, d) * scale)))
+        v0 = np.concatenate([x.real.reshape(-1), x.imag.reshape(-1)])
+        gfd = _fd_grad(L, v0)
+        gfd = gfd[: v0.size // 2] + 1j * gfd[v0.size // 2:]
+        out = np.empty((nx, ny), dtype=np.complex64)
+        with A.Plan.plan2d(1, nx, ny, A.C2C) as p:
+            p.set_norm(norm)
+            p.exec_c2c_adjoint(G.astype(np.complex64), out, d)
+        _fp64_ok(out.reshape(-1), gfd, bound=1e-5, what=("2d adjoint", d))
+
+
 @pytest.mark.parametrize("n", [64, 63])
 def test_adjoint_r2c_against_fd_and_torch(n):
     b = 4
