@@ -193,6 +193,11 @@ struct RagClass {
     int32_t otw_shift; // long: W_L^{k1*n2} = hi[e >> shift] * lo[e & mask]
     int64_t post_off;  // even R2C: W_n^k, k <= n/4 + 1 (float2 offset in the blob)
     int64_t hi_off, lo_off;
+    // pass-table windows [tw_lo, tw_lo + tw_cnt) of ip and ip2, staged in
+    // shared memory after the data buffers at float2 offset tw_smem
+    int64_t tw_lo, tw2_lo;
+    int32_t tw_cnt, tw2_cnt;
+    int32_t tw_smem, tw2_smem;
 };
 
 struct RagXform {

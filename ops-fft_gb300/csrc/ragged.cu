@@ -102,6 +102,17 @@ __device__ __forceinline__ void r2c_post(GetZ getz, const float2* post, float2* 
     }
 }
 
+// Copies a class's pass-table window into shared memory and returns the
+// pointer that makes `tw + pass.tw_off` address it (the window starts at
+// blob offset lo).
+__device__ __forceinline__ const float2* stage_twiddles(const float2* tw, int64_t lo, int cnt, float2* dst)
+{
+    if (cnt <= 0) return tw;
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) dst[i] = ldg2(tw + lo + i);
+    __syncthreads();
+    return dst - lo;
+}
+
 __device__ __forceinline__ bool wait_count(int* ctr, int need, int* err)
 {
     const long long t0 = clock64();
@@ -159,6 +170,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
         const bool odd_r2c = type == RAG_R2C && (C.n & 1);
 
         if (item.kind == RAG_SINGLE) {
+            c.tw = stage_twiddles(tw, C.tw_lo, C.tw_cnt, smem + C.tw_smem);
             const int nthr = C.ip.nthr;
             c.L = C.L;
             c.nthr = nthr;
@@ -198,6 +210,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
                 }
             }
         } else if (item.kind == RAG_P1) {
+            c.tw = stage_twiddles(tw, C.tw_lo, C.tw_cnt, smem + C.tw_smem);
             const int tf = C.group;
             const RagXform x = A.xf[item.xform];
             c.L = C.L1;
@@ -222,6 +235,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
             c.conj_out = false;
             run_passes<RMAX>(c, C.ip, 0, true);
         } else if (item.kind == RAG_P2) {
+            c.tw = stage_twiddles(tw, C.tw2_lo, C.tw2_cnt, smem + C.tw2_smem);
             const int nthr = C.ip2.nthr;
             const RagXform x = A.xf[item.xform];
             c.L = C.L2;
@@ -269,9 +283,13 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
         }
 
         if (item.kind == RAG_P1 || item.kind == RAG_P2) {
-            __threadfence();
+            // release: the CTA barrier orders every thread's stores before
+            // thread 0's fence, which orders them before the counter update
             __syncthreads();
-            if (threadIdx.x == 0) atomicAdd(A.queue + 1 + item.xform, 1);
+            if (threadIdx.x == 0) {
+                __threadfence();
+                atomicAdd(A.queue + 1 + item.xform, 1);
+            }
         }
     }
 }

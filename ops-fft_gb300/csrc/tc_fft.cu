@@ -212,6 +212,55 @@ __host__ __device__ inline size_t smem_bytes_for(int hi_n, int lo_n)
     return (size_t)TcSmem<C>::FIXED + (size_t)(hi_n + lo_n) * 8;
 }
 
+// TF32: the first GEMM's A operand lives in tensor memory (columns
+// [K, 2K) hi, [2K, 3K) lo, after the accumulator [0, K)); BF16 keeps it in
+// shared memory.
+template <class C>
+struct TcTmem {
+    static constexpr bool A_IN_TMEM = !C::BF16;
+    static constexpr int COLS = A_IN_TMEM ? 128 : 32;
+    static constexpr uint32_t A_HI = C::K;
+    static constexpr uint32_t A_LO = 2 * C::K;
+};
+
+// Stage-A operand row half from this thread's R/2 complex values into
+// tensor memory: real parts at K = h*R/2 .., imaginary parts at R + h*R/2 ...
+template <class C>
+__device__ __forceinline__ void put_half_row_tmem(uint32_t trow, int h, const float2* x)
+{
+    float hr[C::HALF], lr[C::HALF], hi[C::HALF], li[C::HALF];
+#pragma unroll
+    for (int j = 0; j < C::HALF; ++j) {
+        hr[j] = tc::to_tf32(x[j].x);
+        lr[j] = tc::to_tf32(x[j].x - hr[j]);
+        hi[j] = tc::to_tf32(x[j].y);
+        li[j] = tc::to_tf32(x[j].y - hi[j]);
+    }
+    const uint32_t kre = (uint32_t)(h * C::HALF), kim = (uint32_t)(C::R + h * C::HALF);
+    tc::tmem_st<C::HALF>(trow + TcTmem<C>::A_HI + kre, hr);
+    tc::tmem_st<C::HALF>(trow + TcTmem<C>::A_HI + kim, hi);
+    tc::tmem_st<C::HALF>(trow + TcTmem<C>::A_LO + kre, lr);
+    tc::tmem_st<C::HALF>(trow + TcTmem<C>::A_LO + kim, li);
+    tc::tmem_wait_st();
+}
+
+// First GEMM with A in tensor memory: D = Ahi*Blo + Alo*Bhi + Ahi*Bhi.
+template <class C>
+__device__ __forceinline__ void issue_gemm_ta(uint32_t tmem, uint32_t bhi, uint32_t blo)
+{
+#pragma unroll
+    for (int kk = 0; kk < C::K / C::KSTEP; ++kk) {
+        const uint32_t ko = (uint32_t)kk * (C::KSTEP / C::EPC) * C::LBO;
+        const uint64_t b_h = tc::sdesc_noswizzle(bhi + ko, C::LBO, C::SBO);
+        const uint64_t b_l = tc::sdesc_noswizzle(blo + ko, C::LBO, C::SBO);
+        const uint32_t a_h = tmem + TcTmem<C>::A_HI + (uint32_t)(kk * C::KSTEP);
+        const uint32_t a_l = tmem + TcTmem<C>::A_LO + (uint32_t)(kk * C::KSTEP);
+        tc::mma_tf32_ta(tmem, a_h, b_l, C::IDESC, kk > 0);
+        tc::mma_tf32_ta(tmem, a_l, b_h, C::IDESC, true);
+        tc::mma_tf32_ta(tmem, a_h, b_h, C::IDESC, true);
+    }
+}
+
 // Per-thread constants of a tile copy.  Interleaved layouts move 16-byte
 // pairs of neighbouring sequences (staging [n][t], pitch TS); contiguous ones
 // 16-byte pairs along each sequence (staging [t][n], pitch P); the generic
@@ -361,7 +410,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_fft_kernel(const TcArgs a)
         fence_mbar_init();
     }
     if (warp == 0) {
-        tc::tmem_alloc(tslot, C::TMEM_COLS);
+        tc::tmem_alloc(tslot, TcTmem<C>::COLS);
         tc::tmem_relinquish();
     }
     tc::fence_async_shared();
@@ -369,7 +418,8 @@ __global__ void __launch_bounds__(kTcThreads) tc_fft_kernel(const TcArgs a)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tslot;
-    const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(hh * C::R);
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+    const uint32_t taddr = trow + (uint32_t)(hh * C::R);
     const uint32_t u_ahi = tc::smem_u32(s_ahi), u_alo = tc::smem_u32(s_alo);
     const uint32_t u_bhi = tc::smem_u32(s_bhi), u_blo = tc::smem_u32(s_blo);
 
@@ -417,13 +467,18 @@ __global__ void __launch_bounds__(kTcThreads) tc_fft_kernel(const TcArgs a)
 #pragma unroll
             for (int j = 0; j < C::HALF; ++j) x[j].y = -x[j].y;
         }
-        put_half_row<C>(s_ahi, s_alo, m, hh, x);
-        tc::fence_async_shared();
+        if constexpr (TcTmem<C>::A_IN_TMEM) {
+            put_half_row_tmem<C>(trow, hh, x);
+        } else {
+            put_half_row<C>(s_ahi, s_alo, m, hh, x);
+            tc::fence_async_shared();
+        }
         tc::fence_before_sync();
         __syncthreads();
         if (tid == 0) {
             tc::fence_after_sync();
-            issue_gemm<C>(tmem, u_ahi, u_alo, u_bhi, u_blo);
+            if constexpr (TcTmem<C>::A_IN_TMEM) issue_gemm_ta<C>(tmem, u_bhi, u_blo);
+            else issue_gemm<C>(tmem, u_ahi, u_alo, u_bhi, u_blo);
             tc::mma_commit(bar);
         }
         failed = !mbar_wait_bounded(bar, phase);
@@ -490,7 +545,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_fft_kernel(const TcArgs a)
     if (failed && tid == 0 && a.err) atomicOr(a.err, 2);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, C::TMEM_COLS);
+    if (warp == 0) tc::tmem_dealloc(tmem, TcTmem<C>::COLS);
 }
 
 // Real-embedded R-point DFT matrix as the B operand, rows in D-column order
@@ -572,7 +627,7 @@ int launch_tc_k(const TcArgs* a, cudaStream_t st)
         const int by_regs = regs_per_warp > 0 ? sm_regs / (regs_per_warp * warps) : 64 / warps;
         int o = by_smem < by_regs ? by_smem : by_regs;
         if (o > 64 / warps) o = 64 / warps;
-        if (o > 512 / C::TMEM_COLS) o = 512 / C::TMEM_COLS;
+        if (o > 512 / TcTmem<C>::COLS) o = 512 / TcTmem<C>::COLS;
         if (o < 1) return (int)cudaErrorInvalidConfiguration;
         occ = o;
     }

@@ -240,16 +240,27 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     double best = -1;
     int best_ng = 0, best_ns = 0;
     int64_t best_gb = 0;
-    for (int nst = 2; nst <= 3; ++nst) {
+    // OPS_FFT_CODELET_NG / OPS_FFT_CODELET_NST pin the groups per CTA and
+    // prefetch stages (tuning experiments); unset, the score below decides
+    const char* env_ng = std::getenv("OPS_FFT_CODELET_NG");
+    const char* env_ns = std::getenv("OPS_FFT_CODELET_NST");
+    const int force_ng = env_ng ? std::atoi(env_ng) : 0;
+    const int force_ns = env_ns ? std::atoi(env_ns) : 0;
+    for (int nst = 2; nst <= 4; ++nst) {
+        if (force_ns ? nst != force_ns : nst > 3) continue;
         const int64_t gb = align(64 + nst * stage_bytes, 128);
         for (int ng = 1; ng <= 15 && ng * cn <= cmaxt; ++ng) {
+            if (force_ng && ng != force_ng) continue;
             const int64_t smem = cta_fixed + ng * gb;
             if (smem > kMaxSmemBytes) break;
             const int64_t warps = (int64_t)ng * cn / 32;
-            // registers: the launch bound caps each thread at 65536 / (MAXT * MINB)
+            // registers: the launch bound caps each thread at 65536 / (MAXT * MINB);
+            // they are allocated per warp in each of the 4 SM sub-partitions
+            // (16384 registers each), so resident warps come in multiples of 4
             const int64_t reg_cap = cmaxt <= 384 ? 80 : 128;
+            const int64_t warps_by_regs = 4 * (16384 / (reg_cap * 32));
             const int64_t ctas = std::min<int64_t>(
-                {(228 * 1024) / (smem + 1024), 64 / warps, 32, 65536 / (reg_cap * 32 * warps)});
+                {(228 * 1024) / (smem + 1024), 64 / warps, 32, warps_by_regs / warps});
             if (ctas < 1) continue;
             int64_t groups_sm = ctas * ng;
             // a small batch cannot keep every group busy
@@ -258,7 +269,10 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
             const double infl =
                 (double)std::min<int64_t>(groups_sm * (nst - 1) * tps * row_bytes, 64 * 1024) / (64 * 1024.0);
             const double score = occ + infl - 0.02 * nst;
-            if (score > best + 1e-9) {
+            // ties: more groups per CTA (up to 384 threads) share the CTA's
+            // twiddle tables and hide each other's barriers (measured faster)
+            const bool tie_better = score > best - 1e-9 && ng > best_ng && ng * cn <= 384;
+            if (score > best + 1e-9 || tie_better) {
                 best = score;
                 best_ng = ng;
                 best_ns = nst;

@@ -30,6 +30,7 @@
 #include <new>
 #include <sstream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "handle.h"
@@ -39,7 +40,8 @@ namespace {
 using namespace gfft;
 
 constexpr int kThreads = 256;
-constexpr int kSmemBudget = 100 * 1024;  // per CTA (two CTAs per SM)
+constexpr int kSmemBudget = 110 * 1024;  // per CTA (two CTAs per SM)
+constexpr int kMaxTwWindow = 5120;       // float2 entries of a pass-table window staged in shared memory
 constexpr int kMaxSingle = 4096;         // longest on-chip complex length
 constexpr int64_t kMaxLength = 1 << 24;
 
@@ -201,13 +203,29 @@ void free_device(aclfftRaggedPlan_t* p)
 
 int ctas_for(aclfftRaggedPlan_t* p, int smem);
 
-// Shared memory an item of the class needs with the chosen variants.
+// Shared memory an item of the class needs with the chosen variants: the
+// data buffers, then the staged pass-table window.
 int class_smem(const RagClass& c)
 {
-    if (c.mode == RAG_MODE_SINGLE) return 2 * c.group * c.pitch * 8;
-    const int p1 = 2 * c.L1 * (c.group + 1) * 8;
-    const int p2 = 2 * c.group2 * c.pitch * 8;
+    if (c.mode == RAG_MODE_SINGLE) return (2 * c.group * c.pitch + c.tw_cnt) * 8;
+    const int p1 = (2 * c.L1 * (c.group + 1) + c.tw_cnt) * 8;
+    const int p2 = (2 * c.group2 * c.pitch + c.tw2_cnt) * 8;
     return std::max(p1, p2);
+}
+
+// Contiguous range of the twiddle blob used by an on-chip plan's passes
+// (cnt = 0 when it is too wide to stage).
+void tw_window(const InnerPlan& ip, int64_t& lo, int32_t& cnt)
+{
+    int64_t a = -1, b = -1;
+    for (int q = 0; q < ip.npass; ++q) {
+        const PassDesc& d = ip.pass[q];
+        if (d.ns <= 1) continue;
+        a = a < 0 ? d.tw_off : std::min<int64_t>(a, d.tw_off);
+        b = std::max<int64_t>(b, d.tw_off + (int64_t)d.ns * d.radix);
+    }
+    lo = a < 0 ? 0 : a;
+    cnt = (a < 0 || b - a > kMaxTwWindow) ? 0 : (int32_t)(b - a);
 }
 
 // Applies candidate choice ch to the class's device descriptor.
@@ -216,24 +234,35 @@ bool apply_choice(ClassPlan& cp, Choice ch)
     RagClass& c = cp.dev;
     if (ch.v1 < 0 || ch.v1 >= (int)cp.ip1.size()) return false;
     c.ip = cp.ip1[ch.v1];
+    tw_window(c.ip, c.tw_lo, c.tw_cnt);
+    c.tw2_lo = 0;
+    c.tw2_cnt = 0;
+    const int budget = kSmemBudget / 8;  // float2 entries
     if (c.mode == RAG_MODE_SINGLE) {
         c.pitch = row_pitch(c.L);
         int g = std::max(1, kThreads / c.ip.nthr);
-        while (g > 1 && 2 * g * c.pitch * 8 > kSmemBudget) --g;
+        while (g > 1 && 2 * g * c.pitch + c.tw_cnt > budget) --g;
+        if (2 * g * c.pitch + c.tw_cnt > budget) c.tw_cnt = 0;
         c.group = g;
         c.group2 = 0;
+        c.tw_smem = 2 * g * c.pitch;
     } else {
         if (ch.v2 < 0 || ch.v2 >= (int)cp.ip2.size()) return false;
         c.ip2 = cp.ip2[ch.v2];
+        tw_window(c.ip2, c.tw2_lo, c.tw2_cnt);
         int g = std::max(1, kThreads / c.ip.nthr);
         g = std::min(g, c.L2);
-        while (g > 1 && 2 * c.L1 * (g + 1) * 8 > kSmemBudget) --g;
+        while (g > 1 && 2 * c.L1 * (g + 1) + c.tw_cnt > budget) --g;
+        if (2 * c.L1 * (g + 1) + c.tw_cnt > budget) c.tw_cnt = 0;
         c.group = g;
+        c.tw_smem = 2 * c.L1 * (g + 1);
         c.pitch = row_pitch(c.L2);
         int g2 = std::max(1, kThreads / c.ip2.nthr);
         g2 = std::min(g2, c.L1);
-        while (g2 > 1 && 2 * g2 * c.pitch * 8 > kSmemBudget) --g2;
+        while (g2 > 1 && 2 * g2 * c.pitch + c.tw2_cnt > budget) --g2;
+        if (2 * g2 * c.pitch + c.tw2_cnt > budget) c.tw2_cnt = 0;
         c.group2 = g2;
+        c.tw2_smem = 2 * g2 * c.pitch;
     }
     cp.choice = ch;
     return class_smem(c) <= kSmemBudget;
@@ -424,31 +453,43 @@ int launch(aclfftRaggedPlan_t* p, const RagArgs& a, cudaStream_t st)
     return gfft_launch_ragged(&a, st);
 }
 
-// Times every candidate of every class on scratch buffers (the class's
-// transforms laid out contiguously) and keeps the fastest.
+// Times every candidate of every class on its own trial batch: m copies of
+// the class's transform (m * n ~ 2^20 points, so a trial launch runs
+// several waves like the real batch does) in scratch buffers, with their
+// own queue, transform table and workspace.  The fastest candidate is kept
+// and cached by (kind, length).
 aclfftResult autotune(aclfftRaggedPlan_t* p)
 {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     load_tune_file();
-    int64_t scratch = 0;
+    constexpr int64_t kTrialPoints = 1 << 20;
+    auto trial_m = [&](const RagClass& c) { return (int)std::min<int64_t>(2048, std::max<int64_t>(4, kTrialPoints / c.n)); };
+    auto ws_per = [](const RagClass& c) -> int64_t {
+        if (c.mode != RAG_MODE_LONG) return 0;
+        return (c.type == RAG_R2C && !(c.n & 1)) ? 2 * (int64_t)c.L : c.L;
+    };
+    int64_t scratch = 16, wsmax = 1;
+    int maxm = 1;
     for (auto& cp : p->classes) {
-        const int64_t m = std::min<int64_t>((int64_t)cp.members.size(), std::max<int64_t>(1, (1 << 18) / cp.dev.n));
-        scratch = std::max<int64_t>(scratch, m * ((int64_t)cp.dev.n + 2) * 8);
+        const int m = trial_m(cp.dev);
+        maxm = std::max(maxm, m);
+        scratch = std::max<int64_t>(scratch, (int64_t)m * ((int64_t)cp.dev.n + 2) * 8);
+        wsmax = std::max<int64_t>(wsmax, (int64_t)m * ws_per(cp.dev));
     }
     void *sin = nullptr, *sout = nullptr;
-    if (cudaMalloc(&sin, (size_t)scratch) != cudaSuccess || cudaMalloc(&sout, (size_t)scratch) != cudaSuccess ||
-        cudaMemset(sin, 0, (size_t)scratch) != cudaSuccess) {
-        cudaGetLastError();
-        if (sin) cudaFree(sin);
-        return ACLFFT_ALLOC_FAILED;
-    }
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    // the class tables and transform table are swapped for sample ones
-    std::vector<RagXform> saved_xf = p->xf;
-    std::vector<int32_t> saved_order = p->order;
-    bool ok = true;
+    int* squeue = nullptr;
+    float2* sws = nullptr;
+    RagXform* sxf = nullptr;
+    int32_t* sorder = nullptr;
+    RagItem* sitems = nullptr;
+    RagClass* scls = nullptr;
+    size_t cap_xf = 0, cap_order = 0, cap_items = 0, cap_cls = 0;
+    bool ok = cudaMalloc(&sin, (size_t)scratch) == cudaSuccess && cudaMalloc(&sout, (size_t)scratch) == cudaSuccess &&
+              cudaMemset(sin, 0, (size_t)scratch) == cudaSuccess &&
+              cudaMalloc(reinterpret_cast<void**>(&squeue), (size_t)(maxm + 1) * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(reinterpret_cast<void**>(&sws), (size_t)wsmax * sizeof(float2)) == cudaSuccess;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
     for (int ci = 0; ci < (int)p->classes.size() && ok; ++ci) {
         ClassPlan& cp = p->classes[ci];
         const Key key{cp.dev.type, cp.dev.n};
@@ -460,57 +501,74 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
         const int n1 = (int)cp.cand1.size();
         const int n2 = cp.dev.mode == RAG_MODE_LONG ? (int)cp.cand2.size() : 1;
         if (n1 * n2 <= 1) continue;
-        const int m = (int)std::min<int64_t>((int64_t)cp.members.size(), std::max<int64_t>(1, (1 << 18) / cp.dev.n));
-        // sample transforms: contiguous, ws reused from the plan's workspace
-        std::vector<RagXform> sx(p->count);
-        int64_t ws_cursor = 0;
+        const int m = trial_m(cp.dev);
+        // the trial batch: one class (index 0), m transforms packed in scratch
+        aclfftRaggedPlan_t tmp;
+        tmp.count = m;
+        tmp.xf.resize(m);
         for (int k = 0; k < m; ++k) {
-            RagXform x{};
+            RagXform& x = tmp.xf[k];
             x.in_off = (int64_t)k * ((int64_t)cp.dev.n + 2) * 8;
             x.out_off = x.in_off;
-            x.cls = ci;
-            if (cp.dev.mode == RAG_MODE_LONG) {
-                x.ws_off = ws_cursor;
-                ws_cursor += (cp.dev.type == RAG_R2C && !(cp.dev.n & 1)) ? 2 * (int64_t)cp.dev.L : cp.dev.L;
-            }
-            sx[cp.members[k]] = x;
+            x.ws_off = (int64_t)k * ws_per(cp.dev);
+            x.cls = 0;
         }
-        if (ws_cursor > p->ws_floats2) continue;
         double best = 1e30;
         Choice bestc = cp.choice;
         for (int a1 = 0; a1 < n1 && ok; ++a1)
             for (int a2 = 0; a2 < n2 && ok; ++a2) {
                 if (!apply_choice(cp, {a1, a2})) continue;
-                // items of this class only, for the sample transforms
-                aclfftRaggedPlan_t tmp;
-                tmp.count = p->count;
-                tmp.classes = p->classes;
-                for (auto& c2 : tmp.classes) c2.members.clear();
-                tmp.classes[ci].members.assign(cp.members.begin(), cp.members.begin() + m);
+                tmp.classes.assign(1, cp);
+                tmp.classes[0].members.resize(m);
+                for (int k = 0; k < m; ++k) tmp.classes[0].members[k] = k;
                 build_items(&tmp);
-                p->xf = sx;
-                p->order = tmp.order;
-                std::vector<RagClass> cls;
-                for (auto& c2 : p->classes) cls.push_back(c2.dev);
-                RagItem* ditems = nullptr;
-                if (!upload(p->d_cls, cls) || !upload(p->d_xf, p->xf) || !upload(p->d_order, p->order) ||
-                    !upload(ditems, tmp.items)) {
-                    if (ditems) cudaFree(ditems);
+                std::vector<RagClass> cls(1, cp.dev);
+                // trial tables: reallocated only when they grow
+                auto put = [&](auto*& d, size_t& cap, const auto& h) {
+                    using T = typename std::decay_t<decltype(h)>::value_type;
+                    if (h.size() > cap) {
+                        if (d) cudaFree(d);
+                        d = nullptr;
+                        cap = 0;
+                        if (cudaMalloc(reinterpret_cast<void**>(&d), h.size() * sizeof(T)) != cudaSuccess) return false;
+                        cap = h.size();
+                    }
+                    return h.empty() ||
+                           cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+                };
+                if (!put(scls, cap_cls, cls) || !put(sxf, cap_xf, tmp.xf) || !put(sorder, cap_order, tmp.order) ||
+                    !put(sitems, cap_items, tmp.items)) {
                     ok = false;
                     break;
                 }
-                const RagArgs ra = make_args(p, ditems, (int)tmp.items.size(), tmp.smem, sin, sout, false);
+                RagArgs ra{};
+                ra.cls = scls;
+                ra.xf = sxf;
+                ra.order = sorder;
+                ra.items = sitems;
+                ra.nitems = (int)tmp.items.size();
+                ra.smem_bytes = tmp.smem;
+                ra.ctas = ctas_for(p, tmp.smem);
+                ra.queue = squeue;
+                ra.err = p->d_err;
+                ra.tw = p->tw;
+                ra.in = sin;
+                ra.out = sout;
+                ra.ws = sws;
+                ra.scale_c2c = 1.f;
+                if (ra.ctas <= 0) {
+                    ok = false;
+                    break;
+                }
                 float tbest = 1e30f;
-                for (int rep = 0; rep < 4 && ok; ++rep) {
-                    cudaEventRecord(e0, p->s_cap);
-                    if (launch(p, ra, p->s_cap) != 0) ok = false;
-                    cudaEventRecord(e1, p->s_cap);
-                    if (cudaEventSynchronize(e1) != cudaSuccess) ok = false;
+                for (int rep = 0; rep < 3 && ok; ++rep) {
+                    ok = cudaMemsetAsync(squeue, 0, (size_t)(m + 1) * sizeof(int), p->s_cap) == cudaSuccess &&
+                         cudaEventRecord(e0, p->s_cap) == cudaSuccess && gfft_launch_ragged(&ra, p->s_cap) == 0 &&
+                         cudaEventRecord(e1, p->s_cap) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess;
                     float ms = 0;
-                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ok) cudaEventElapsedTime(&ms, e0, e1);
                     if (rep > 0) tbest = std::min(tbest, ms);
                 }
-                cudaFree(ditems);
                 if (tbest < best) {
                     best = tbest;
                     bestc = {a1, a2};
@@ -521,15 +579,13 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
         cp.tuned = true;
         g_tuned[key] = bestc;
     }
-    p->xf = saved_xf;
-    p->order = saved_order;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(sin);
-    cudaFree(sout);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    for (void* q : {(void*)sin, (void*)sout, (void*)squeue, (void*)sws, (void*)sxf, (void*)sorder, (void*)sitems,
+                    (void*)scls})
+        if (q) cudaFree(q);
     if (!ok) {
         cudaGetLastError();
-        // back to the untuned variants, tables restored
         for (auto& cp : p->classes) {
             apply_choice(cp, {0, 0});
             cp.tuned = false;
@@ -835,6 +891,19 @@ ACLFFT_API int aclfftRaggedDebugCheck(aclfftRaggedPlan plan, char* msg, int msgl
             return ip.nthr >= 1 && ip.nthr <= kThreads;
         };
         if (!tw_ok(c.ip)) return report("pass tables / threads", 3);
+        if (c.tw_cnt < 0 || c.tw_lo + c.tw_cnt > twn || c.tw2_cnt < 0 || c.tw2_lo + c.tw2_cnt > twn)
+            return report("staged twiddle window", 3);
+        auto window_covers = [](const InnerPlan& ip, int64_t lo, int cnt) {
+            if (cnt == 0) return true;
+            for (int q = 0; q < ip.npass; ++q)
+                if (ip.pass[q].ns > 1 &&
+                    (ip.pass[q].tw_off < lo || ip.pass[q].tw_off + (int64_t)ip.pass[q].ns * ip.pass[q].radix > lo + cnt))
+                    return false;
+            return true;
+        };
+        if (!window_covers(c.ip, c.tw_lo, c.tw_cnt) ||
+            (c.mode == RAG_MODE_LONG && !window_covers(c.ip2, c.tw2_lo, c.tw2_cnt)))
+            return report("staged window misses a pass table", 3);
         if (c.post_off >= 0 && c.post_off + c.L / 2 + 1 > twn) return report("post table", 3);
         if (it.kind == RAG_SINGLE) {
             if (c.group * c.ip.nthr > kThreads || it.count < 1 || it.count > c.group) return report("single group", 4);
