@@ -44,6 +44,10 @@ FALLBACK_HBM_GBS = 6800.0
 # the algorithmic read+write bytes.
 NCU_TRAFFIC = {
     ("cfg2", "dominant"): 52794112,  # R2C N=3000 batch=4096: 49.22 MB read + 3.58 MB written
+    ("cfg1", "dominant"): 8475904,   # C2C 4096 x 256: 8.48 MB read (the 16.8 MB of data fit in L2)
+    ("cfg3", "dominant"): 68792064,  # TF32x3 N=65536 x 64, both passes: 67.19 MB read + 1.60 MB written
+    ("cfg4", "dominant"): 972500000,  # 2D forward: row pass 268.5 + 225.4 MB, column pass 268.5 + 210.1 MB
+    ("cfg5", "dominant"): 1086378752,  # ragged launch: 567.78 MB read + 518.60 MB written (workspace round trip)
 }
 
 
@@ -403,6 +407,8 @@ class Cfg5:
     integers in [16, 32768], 70% C2C / 30% R2C, x ~ N(0,1), one persistent
     launch per step (replayed CUDA graph, autotuned per-length plans)."""
 
+    untuned = False
+
     def __init__(self, torch, A, dev, stream, nsets):
         import numpy as np
 
@@ -411,6 +417,8 @@ class Cfg5:
         self.ino, self.outo, ci, co = A.ragged_layout(self.lengths, self.types)
         self.plan = A.RaggedPlan(self.lengths, self.types, self.ino, self.outo)
         self.plan.set_stream(stream)
+        if Cfg5.untuned:
+            self.plan.set_options(autotune=False, graph=False)
         g = torch.Generator(device="cpu").manual_seed(12345)
         self.sets = []
         for _ in range(nsets):
@@ -554,8 +562,11 @@ def main():
     ap.add_argument("--workload", default="cfg2")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ragged-untuned", action="store_true",
+                    help="cfg5: no autotuning and no graph replay (kernel profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    Cfg5.untuned = args.ragged_untuned
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
