@@ -360,10 +360,10 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             group_sync(bar_id, S::NTHR);
             from_slot = false;
         }
-        codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off - A.tw_lo, from_slot, last_global, bar_id);
+        codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off, from_slot, last_global, bar_id);
         sfor<S::NP - 1>([&](auto pp) {
             constexpr int P = decltype(pp)::value + 1;
-            codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off - A.tw_lo, false, last_global, bar_id);
+            codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off, false, last_global, bar_id);
         });
         if (A.io_mode == IO_R2C_EVEN) {
             // post-process pairs:
@@ -396,6 +396,88 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                 issue(s, nt);
             }
         }
+    }
+}
+
+// Column tiles: tfpc adjacent columns of a strided axis (column c, element
+// r at base(c) + r*in_stride, base as in the column kernel) per tile, one
+// codelet transform group per column.  The tile is loaded cooperatively
+// (consecutive threads take consecutive columns of a row, so every row of
+// the tile is one contiguous HBM segment), each group runs the codelet's
+// in-place passes on its column, and the tile is stored back the same way.
+// Persistent over tiles; in-place calls are safe (a tile is fully read
+// before it is written).
+template <class S>
+__global__ void __launch_bounds__(S::MAXT, S::MINB) coltile_kernel(const __grid_constant__ ColArgs A)
+{
+    extern __shared__ __align__(128) unsigned char smraw[];
+    constexpr int L = S::L;
+    const int TF = A.tfpc;
+    const int g = threadIdx.x / S::NTHR;
+    const int tid = threadIdx.x - g * S::NTHR;
+    const int bar_id = 1 + g;
+    float2* stw = reinterpret_cast<float2*>(smraw);
+    float2* tile = reinterpret_cast<float2*>(smraw + (((int64_t)A.tw_cnt * 8 + 127) & ~(int64_t)127));
+    const float2* gtw = reinterpret_cast<const float2*>(A.tw);
+    for (int i = threadIdx.x; i < A.tw_cnt; i += blockDim.x) stw[i] = ldg2(gtw + A.tw_lo + i);
+    const float2* tw = A.tw_cnt > 0 ? stw - A.tw_lo : gtw;
+    __syncthreads();
+
+    PipeCtx c;
+    c.L = L;
+    c.nthr = S::NTHR;
+    c.tid = tid;
+    c.ok_sm = true;
+    c.ok_io = true;
+    c.pshift = S::PSHIFT;
+    c.tw = tw;
+    c.mode = IO_C2C;
+    c.conj_in = 0;
+    c.conj_out = 0;
+    c.scale = 1.f;
+    float2 v[S::E];
+    float2* W = tile + (int64_t)g * A.wsize;
+
+    // this thread's column within a tile and its first row; rows step by NTHR
+    const int cc = threadIdx.x % TF;
+    const int r0 = threadIdx.x / TF;
+    const int rstep = blockDim.x / TF;
+    const int64_t ntiles = (A.ncols + TF - 1) / TF;
+    const float2* gin = reinterpret_cast<const float2*>(A.in);
+    float2* gout = reinterpret_cast<float2*>(A.out);
+    const float sc = A.scale;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t col = t * TF + cc;
+        const bool ok = col < A.ncols;
+        const int64_t cl = ok ? col : 0;
+        const int64_t item = cl / A.cpi;
+        const int64_t j = cl - item * A.cpi;
+        const float2* ib = gin + item * A.in_dist + (j / A.in_split) * A.in_hi + (j % A.in_split) * A.in_lo;
+        float2* ob = gout + item * A.out_dist + (j / A.out_split) * A.out_hi + (j % A.out_split) * A.out_lo;
+        float2* Wc = tile + (int64_t)cc * A.wsize;
+        if (ok) {
+            for (int r = r0; r < L; r += rstep) {
+                float2 x = ldg2(ib + (int64_t)r * A.in_stride);
+                if (A.conj_in) x.y = -x.y;
+                Wc[cpad<S>(r)] = x;
+            }
+        }
+        __syncthreads();
+        if (g < TF) {
+            sfor<S::NP>([&](auto pp) {
+                constexpr int P = decltype(pp)::value;
+                codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off, false, false, bar_id);
+            });
+        }
+        __syncthreads();
+        if (ok) {
+            for (int r = r0; r < L; r += rstep) {
+                float2 x = Wc[cpad<S>(r)];
+                if (A.conj_out) x.y = -x.y;
+                ob[(int64_t)r * A.out_stride] = sc == 1.f ? x : cscale(x, sc);
+            }
+        }
+        __syncthreads();
     }
 }
 

@@ -8,6 +8,10 @@ namespace gfft {
     int launch_codelet_##ID(const RowArgs* a, cudaStream_t st)                           \
     {                                                                                    \
         return launch_codelet_t<CSpec<MT, MB, L, NT, __VA_ARGS__>>(a, st);                       \
+    }                                                                                    \
+    int launch_coltile_##ID(const ColArgs* a, cudaStream_t st)                           \
+    {                                                                                    \
+        return launch_coltile_t<CSpec<MT, MB, L, NT, __VA_ARGS__>>(a, st);                       \
     }
 #define GFFT_PICK(ID, MT, MB, L, NT, ...) GFFT_PICK_##ID(ID, MT, MB, L, NT, __VA_ARGS__)
 #define GFFT_PICK_6(ID, MT, MB, L, NT, ...) GFFT_INST(ID, MT, MB, L, NT, __VA_ARGS__)

@@ -104,6 +104,18 @@ extern "C" int gfft_launch_row(const RowArgs* a, void* stream)
 extern "C" int gfft_launch_col(const ColArgs* a, void* stream)
 {
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (a->codelet) {
+    case -1: break;
+    case 0: return launch_coltile_0(a, st);
+    case 1: return launch_coltile_1(a, st);
+    case 2: return launch_coltile_2(a, st);
+    case 3: return launch_coltile_3(a, st);
+    case 4: return launch_coltile_4(a, st);
+    case 5: return launch_coltile_5(a, st);
+    case 6: return launch_coltile_6(a, st);
+    case 7: return launch_coltile_7(a, st);
+    default: return (int)cudaErrorInvalidValue;
+    }
     switch (a->ip.rmax) {
     case 16: return launch_col_r16(a, st);
     case 47: return launch_col_r47(a, st);

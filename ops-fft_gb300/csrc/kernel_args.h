@@ -112,6 +112,15 @@ struct ColArgs {
     int32_t conj_out;
     int32_t staged_out;  // output of column c is out + c*L + k (contiguous blocks)
     float scale;
+    // column-tile codelet (codelet >= 0): tfpc adjacent columns per tile, one
+    // codelet transform group per column, column g held at g*wsize in shared
+    // memory after the pass-table window [tw_lo, tw_lo + tw_cnt)
+    int32_t codelet;
+    int32_t tw_lo;
+    int32_t tw_cnt;
+    int32_t wsize;
+    int32_t smem_bytes;
+    int32_t pad2_;
 };
 
 // Stand-alone even/odd packing for R2C/C2R lengths beyond one CTA.

@@ -107,6 +107,41 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
     return (int)cudaGetLastError();
 }
 
+template <class S>
+int launch_coltile_t(const ColArgs* a, cudaStream_t st)
+{
+    static unsigned long long attr_mask = 0;
+    static thread_local int last_threads = -1, last_smem = -1, last_occ = 1;
+    const int threads = S::NTHR * a->tfpc;
+    if (a->ip.L != S::L || a->tfpc < 1 || threads > S::MAXT || a->ncols <= 0 || a->wsize <= 0)
+        return (int)cudaErrorInvalidValue;
+    if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes) return (int)cudaErrorInvalidValue;
+    cudaError_t e = ensure_smem_attr(coltile_kernel<S>, attr_mask, (size_t)a->smem_bytes);
+    if (e != cudaSuccess) return (int)e;
+    if (threads != last_threads || a->smem_bytes != last_smem) {
+        int occ = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, coltile_kernel<S>, threads, (size_t)a->smem_bytes);
+        if (e != cudaSuccess) return (int)e;
+        last_threads = threads;
+        last_smem = a->smem_bytes;
+        last_occ = occ < 1 ? 1 : occ;
+    }
+    const int64_t ntiles = (a->ncols + a->tfpc - 1) / a->tfpc;
+    int64_t grid = (int64_t)sm_count() * last_occ;
+    if (grid < 1) grid = 1;
+    if (grid > ntiles) grid = ntiles;
+    coltile_kernel<S><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
+    return (int)cudaGetLastError();
+}
+
+int launch_coltile_0(const ColArgs* a, cudaStream_t st);
+int launch_coltile_1(const ColArgs* a, cudaStream_t st);
+int launch_coltile_2(const ColArgs* a, cudaStream_t st);
+int launch_coltile_3(const ColArgs* a, cudaStream_t st);
+int launch_coltile_4(const ColArgs* a, cudaStream_t st);
+int launch_coltile_5(const ColArgs* a, cudaStream_t st);
+int launch_coltile_6(const ColArgs* a, cudaStream_t st);
+int launch_coltile_7(const ColArgs* a, cudaStream_t st);
 int launch_codelet_0(const RowArgs* a, cudaStream_t st);
 int launch_codelet_1(const RowArgs* a, cudaStream_t st);
 int launch_codelet_2(const RowArgs* a, cudaStream_t st);

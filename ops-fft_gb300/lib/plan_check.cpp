@@ -155,10 +155,33 @@ bool check_col(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const ColArgs& a = s.col;
     if (!check_inner(a.ip, tw_count, why)) return false;
     const int L = a.ip.L;
-    const int maxthr = a.ip.rmax == 16 ? 512 : 256;
-    if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1 || a.tfp < a.tfpc) return fail(why, "col threads");
-    if ((int64_t)a.nbuf * L * a.tfp * 8 > kMaxSmemBytes) return fail(why, "col smem");
-    if (buffers_used(a.ip.npass, 0, !a.staged_out) > a.nbuf) return fail(why, "col needs more shared buffers");
+    if (a.codelet >= 0) {
+        // column-tile codelet: the codelet's compile-time spec must match the plan
+        int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
+        if (gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt) != a.codelet) return fail(why, "coltile codelet id");
+        if (cn != a.ip.nthr || cnr != a.ip.npass) return fail(why, "coltile spec");
+        for (int q = 0; q < cnr; ++q)
+            if (cr[q] != a.ip.pass[q].radix) return fail(why, "coltile radices");
+        if (a.tfpc < 1 || a.tfpc * cn > cmaxt) return fail(why, "coltile threads");
+        const int pshift = (cr[0] % 2 == 0) ? 4 : 30;
+        const int64_t need = (int64_t)(L - 1) + ((int64_t)(L - 1) >> pshift) + 1;
+        if (a.wsize < need) return fail(why, "coltile column region");
+        const int64_t tw_bytes = ((int64_t)a.tw_cnt * 8 + 127) & ~(int64_t)127;
+        if (tw_bytes + (int64_t)a.tfpc * a.wsize * 8 > a.smem_bytes || a.smem_bytes > kMaxSmemBytes)
+            return fail(why, "coltile smem");
+        if (a.tw_cnt < 0 || a.tw_lo < 0 || a.tw_lo + (int64_t)a.tw_cnt > tw_count) return fail(why, "coltile tw window");
+        for (int q = 0; q < a.ip.npass; ++q)
+            if (a.ip.pass[q].ns > 1 && a.tw_cnt > 0 &&
+                (a.ip.pass[q].tw_off < a.tw_lo ||
+                 a.ip.pass[q].tw_off + (int64_t)a.ip.pass[q].ns * a.ip.pass[q].radix > (int64_t)a.tw_lo + a.tw_cnt))
+                return fail(why, "coltile tw window misses a pass table");
+        if (a.ons > 1 || a.staged_out) return fail(why, "coltile with outer twiddles or staged output");
+    } else {
+        const int maxthr = a.ip.rmax == 16 ? 512 : 256;
+        if (a.ip.nthr * a.tfpc > maxthr || a.tfpc < 1 || a.tfp < a.tfpc) return fail(why, "col threads");
+        if ((int64_t)a.nbuf * L * a.tfp * 8 > kMaxSmemBytes) return fail(why, "col smem");
+        if (buffers_used(a.ip.npass, 0, !a.staged_out) > a.nbuf) return fail(why, "col needs more shared buffers");
+    }
     if ((a.ncols + a.tfpc - 1) / a.tfpc > 0x7fffffff) return fail(why, "col grid");
     if (a.cpi < 1 || a.ncols % a.cpi != 0) return fail(why, "col cpi");
     const int64_t items = a.ncols / a.cpi;
