@@ -74,6 +74,7 @@ class PlanInfo(ctypes.Structure):
         ("stages", ctypes.c_int),
         ("smem_bytes", ctypes.c_int),
         ("tc_stages", ctypes.c_int),
+        ("cluster_ctas", ctypes.c_int),
     ]
 
 

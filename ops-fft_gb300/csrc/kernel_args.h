@@ -245,6 +245,34 @@ struct RagArgs {
     float scale_c2c;  // applied to C2C outputs
 };
 
+// Long C2C transforms on a thread-block cluster (csrc/cluster_fft.cu).  The
+// length N = Q*P is split over the C CTAs of one cluster: CTA c loads the
+// columns [c*P/C, (c+1)*P/C) of the Q x P row-major view of the input, runs
+// the Q-point column transforms and the W_N^{p*k_q} twiddle, and stores each
+// (Q/C) x (P/C) block into the shared memory of the CTA that owns those rows;
+// CTA d then runs the P-point transforms of rows [d*Q/C, (d+1)*Q/C) and
+// writes bins k_q + Q*k_p.  One HBM read and one HBM write per element.
+// Transform t reads in + t*in_dist and writes out + t*out_dist (float2
+// units); the clusters are persistent over transforms.
+struct ClusterArgs {
+    const void* in;
+    void* out;
+    const void* tw;     // twiddle blob
+    int64_t ntf;        // transforms
+    int64_t in_dist, out_dist;
+    int64_t twq_off;    // blob offset: column-phase second-pass table, W_Q^{k*r} at r*Q0 + k
+    int64_t twp_off;    // blob offset: row-phase second-pass table, W_P^{k*r} at r*P0 + k
+    int64_t outer_off;  // blob offset: W_N^e, e < N
+    int32_t kid;        // configuration id (csrc/cluster_list.h)
+    int32_t csize;      // CTAs per cluster (must match the configuration)
+    int32_t conj_in;
+    int32_t conj_out;
+    float scale;
+    int32_t smem_bytes;
+    int32_t clusters;   // co-resident clusters (set when the plan is prepared on a device)
+    int32_t pad_;
+};
+
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
 //   kind 1: f(i) = (i * mult) mod M               (linear tables)
 //   kind 2: f(i) = ((i / ns) * (i % ns)) mod M    (pass tables, [r][k] layout)
@@ -268,6 +296,15 @@ int gfft_launch_col(const gfft::ColArgs* a, void* stream);
 int gfft_launch_pack(const gfft::PackArgs* a, void* stream);
 int gfft_launch_tc(const gfft::TcArgs* a, void* stream);
 int gfft_launch_ragged(const gfft::RagArgs* a, void* stream);
+int gfft_launch_cluster(const gfft::ClusterArgs* a, void* stream);
+// Cluster configuration for length n (csrc/cluster_list.h): returns its id
+// (or -1) and fills the cluster size, the column/row lengths, their first
+// radices, the threads per CTA and the dynamic shared memory per CTA.  want_c > 0 selects that cluster size.
+int gfft_cluster_lookup(long long n, int want_c, int* csize, int* q, int* p, int* q0, int* p0, int* nt, int* smem_bytes);
+// Sets the kernel attributes of configuration kid on the current device and
+// returns how many of its clusters are co-resident (negative CUDA error on
+// failure).  Not stream-ordered: call outside stream capture.
+int gfft_cluster_prepare(int kid);
 // Prepares the ragged kernel for a shared-memory size (attributes) and
 // returns its resident CTAs per SM (0 on error).  Not stream-ordered: call
 // outside stream capture.

@@ -116,6 +116,17 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
             if (last) s.tc.scale = scale;
             rc = gfft_launch_tc(&s.tc, st);
             break;
+        case Step::CLUSTER:
+            s.cl.in = src;
+            s.cl.out = dst;
+            s.cl.tw = tw;
+            if (c2c) {
+                s.cl.conj_in = first && inverse;
+                s.cl.conj_out = last && inverse;
+            }
+            if (last) s.cl.scale = scale;
+            rc = gfft_launch_cluster(&s.cl, st);
+            break;
         }
         if (rc != 0) {
             gfft::set_last_error(std::string("kernel launch failed: ") + cudaGetErrorString((cudaError_t)rc));

@@ -228,6 +228,22 @@ aclfftResult plan_device_setup(PlanImpl* p)
             return ACLFFT_SETUP_FAILED;
         }
     }
+    // cluster kernels: attributes and co-resident clusters, once per plan
+    // (outside any stream capture)
+    for (StepList& sl : p->lists) {
+        for (Step& s : sl.steps) {
+            if (s.kind != Step::CLUSTER) continue;
+            const int n = gfft_cluster_prepare(s.cl.kid);
+            if (n < 1) {
+                cudaGetLastError();
+                plan_impl_free(p);
+                set_last_error(std::string("cluster kernel setup failed: ") +
+                               cudaGetErrorString((cudaError_t)(n < 0 ? -n : (int)cudaErrorInvalidConfiguration)));
+                return ACLFFT_SETUP_FAILED;
+            }
+            s.cl.clusters = n;
+        }
+    }
     p->device = dev;
     p->device_ready = true;
     return ACLFFT_SUCCESS;

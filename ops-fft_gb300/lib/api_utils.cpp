@@ -150,6 +150,8 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
     info->nsteps = (int)sl.steps.size();
     for (const gfft::Step& s : sl.steps)
         if (s.kind == gfft::Step::TC) ++info->tc_stages;
+    for (const gfft::Step& s : sl.steps)
+        if (s.kind == gfft::Step::CLUSTER) info->cluster_ctas = s.cl.csize;
     for (const gfft::Step& s : sl.steps) {
         const gfft::InnerPlan* ip = nullptr;
         int tf = 0;
@@ -164,6 +166,22 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
         } else if (s.kind == gfft::Step::COL) {
             ip = &s.col.ip;
             tf = s.col.tfpc;
+        } else if (s.kind == gfft::Step::CLUSTER) {
+            // column radices then row radices; threads = all CTAs of a cluster
+            int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
+            const long long n = plan->rank == 2 ? 0 : (long long)plan->lengths[0];
+            if (gfft_cluster_lookup(n, s.cl.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) == s.cl.kid) {
+                info->nradix = 4;
+                info->radix[0] = Q0;
+                info->radix[1] = Q / Q0;
+                info->radix[2] = P0;
+                info->radix[3] = P / P0;
+                info->onchip_length = Q * P;
+                info->threads_per_transform = nt * C;
+                info->transforms_per_cta = 1;
+                info->smem_bytes = smem;
+            }
+            break;
         }
         if (!ip) continue;
         info->nradix = ip->npass;

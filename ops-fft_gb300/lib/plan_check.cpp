@@ -270,6 +270,35 @@ bool check_tc(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     return true;
 }
 
+// Cluster transform: the configuration matches the length, every HBM
+// access of the column loads and row stores, the twiddle ranges and the
+// receive-buffer offsets of the distributed shared-memory stores.
+bool check_cluster(const Step& s, const Bufs& b, int64_t n, int64_t tw_count, std::string& why)
+{
+    const ClusterArgs& a = s.cl;
+    int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
+    if (gfft_cluster_lookup(n, a.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) != a.kid) return fail(why, "cluster config");
+    if ((int64_t)Q * P != n || P % C || Q % C) return fail(why, "cluster split");
+    if (smem != a.smem_bytes || smem > kMaxSmemBytes) return fail(why, "cluster shared memory");
+    if (a.ntf < 1 || a.in_dist < n || a.out_dist < n) return fail(why, "cluster sizes");
+    const int64_t ein = b.bytes[s.src] / 8, eout = b.bytes[s.dst] / 8;
+    if ((a.ntf - 1) * a.in_dist + (int64_t)(Q - 1) * P + (P - 1) >= ein) return fail(why, "cluster load out of bounds");
+    if ((a.ntf - 1) * a.out_dist + (Q - 1) + (int64_t)Q * (P - 1) >= eout)
+        return fail(why, "cluster store out of bounds");
+    if (a.twq_off < 0 || a.twq_off + Q > tw_count || a.twp_off < 0 || a.twp_off + P > tw_count)
+        return fail(why, "cluster pass tables out of table");
+    if (a.outer_off < 0 || a.outer_off + n > tw_count) return fail(why, "cluster outer twiddles out of table");
+    if ((int64_t)(P - 1) * (Q - 1) >= n) return fail(why, "cluster outer twiddle index");
+    const int PC = P / C, QC = Q / C, RP = P + 1;
+    for (int rank = 0; rank < C; ++rank)
+        for (int kq = 0; kq < Q; ++kq) {
+            const int d = kq / QC, kl = kq % QC;
+            const int64_t off = (int64_t)kl * RP + rank * PC + (PC - 1);
+            if (d >= C || off >= (int64_t)QC * RP) return fail(why, "cluster exchange offset");
+        }
+    return true;
+}
+
 }  // namespace
 
 extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int msglen)
@@ -320,6 +349,7 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
             else if (s.kind == Step::COL) ok = check_col(s, b, impl->tb.count, why);
             else if (s.kind == Step::PACK) ok = check_pack(s, b, impl->tb.count, why);
             else if (s.kind == Step::TC) ok = check_tc(s, b, impl->tb.count, why);
+            else if (s.kind == Step::CLUSTER) ok = check_cluster(s, b, p.n0, impl->tb.count, why);
             else if (s.kind == Step::COPY)
                 ok = (s.copy_bytes <= b.bytes[s.src] && s.copy_bytes <= b.bytes[s.dst]) || fail(why, "copy size");
             if (!ok) {

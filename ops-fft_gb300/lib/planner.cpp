@@ -191,6 +191,15 @@ bool codelets_enabled()
 }
 int col_max_length() { return 2048; }
 
+bool clusters_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("OPS_FFT_CLUSTER");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 namespace {
 
 // Codelet row step (see csrc/codelet.cuh for the execution model and the
@@ -532,6 +541,34 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     return true;
 }
 
+// Whole batched C2C of length n on thread-block clusters (one cluster per
+// transform, see csrc/cluster_fft.cu).  False when no configuration exists.
+bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st)
+{
+    if (!clusters_enabled() || n > 0x7fffffff) return false;
+    const char* env_c = std::getenv("OPS_FFT_CLUSTER_C");
+    const int want_c = env_c ? std::atoi(env_c) : 0;
+    int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
+    const int kid = gfft_cluster_lookup(n, want_c, &C, &Q, &P, &Q0, &P0, &nt, &smem);
+    if (kid < 0) return false;
+    st = Step{};
+    st.kind = Step::CLUSTER;
+    ClusterArgs& a = st.cl;
+    a.kid = kid;
+    a.csize = C;
+    a.ntf = batch;
+    a.in_dist = n;
+    a.out_dist = n;
+    a.twq_off = tb.add_pass_table(Q0, Q / Q0);
+    a.twp_off = tb.add_pass_table(P0, P / P0);
+    a.outer_off = tb.add_linear(n, n, 1);
+    a.scale = 1.f;
+    a.smem_bytes = smem;
+    a.clusters = 0;
+    st.tw_off = 0;
+    return true;
+}
+
 // Strided-axis transform as a list of column passes with buffer routing.
 bool make_axis_steps(int64_t n, int64_t S, int64_t items, int64_t D, int src, int dst, int spare, int cap,
                      TwiddleBuilder& tb, std::vector<Step>& out, bool& needs_spare)
@@ -785,6 +822,15 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
                 return unsupported("vertical length not decomposable");
             if (spare) need_ws(N * p.stride * 8);
             return true;
+        }
+        {
+            Step st;
+            if (make_cluster_step(N, p.batch, tb, st)) {
+                st.src = IN;
+                st.dst = BUF_OUT;
+                out.steps.push_back(st);
+                return true;
+            }
         }
         if (N <= row_max_length() && row_feasible((int)N, IO_C2C)) {
             Step st;

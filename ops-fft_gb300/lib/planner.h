@@ -28,6 +28,10 @@ int col_max_length();
 // Compile-time specialised row kernels are used unless OPS_FFT_CODELETS=0.
 bool codelets_enabled();
 
+// Long C2C lengths with a cluster configuration run on thread-block
+// clusters unless OPS_FFT_CLUSTER=0.
+bool clusters_enabled();
+
 // Radix sequence for an on-chip transform of length L (product == L),
 // radices <= 16 when possible, primes up to 47 otherwise.  Empty on failure.
 std::vector<int> choose_radices(int L);
@@ -38,12 +42,13 @@ std::vector<int> split_axis(int64_t n, int cap);
 enum BufId : int { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_WS2 = 3 };
 
 struct Step {
-    enum Kind { ROW, COL, PACK, COPY, TC } kind = ROW;
+    enum Kind { ROW, COL, PACK, COPY, TC, CLUSTER } kind = ROW;
     int64_t copy_bytes = 0;
     RowArgs row{};
     ColArgs col{};
     PackArgs pack{};
     TcArgs tc{};
+    ClusterArgs cl{};
     int src = BUF_IN;
     int dst = BUF_OUT;
     // Offsets (float2 units) into the plan's twiddle blob for the pointers
