@@ -80,6 +80,7 @@ typedef struct aclfftPlanInfo_t {
     int smem_bytes;            /* dynamic shared memory per CTA */
     int tc_stages;             /* tensor-core DFT-matrix launches per exec (0: FP32 kernels only) */
     int cluster_ctas;          /* CTAs per thread-block cluster of a cluster transform (0: none) */
+    int cluster_count;         /* clusters resident at once on the plan's device (0: not prepared) */
 } aclfftPlanInfo;
 
 ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info);

@@ -75,6 +75,7 @@ class PlanInfo(ctypes.Structure):
         ("smem_bytes", ctypes.c_int),
         ("tc_stages", ctypes.c_int),
         ("cluster_ctas", ctypes.c_int),
+        ("cluster_count", ctypes.c_int),
     ]
 
 

@@ -258,6 +258,7 @@ struct ClusterArgs {
     const void* in;
     void* out;
     const void* tw;     // twiddle blob
+    int* err;           // device error word (bit 3: an exchange wait timed out)
     int64_t ntf;        // transforms
     int64_t in_dist, out_dist;
     int64_t twq_off;    // blob offset: column-phase second-pass table, W_Q^{k*r} at r*Q0 + k

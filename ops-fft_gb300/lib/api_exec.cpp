@@ -120,6 +120,7 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
             s.cl.in = src;
             s.cl.out = dst;
             s.cl.tw = tw;
+            s.cl.err = impl->err;
             if (c2c) {
                 s.cl.conj_in = first && inverse;
                 s.cl.conj_out = last && inverse;

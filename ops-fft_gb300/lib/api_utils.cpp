@@ -151,7 +151,10 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
     for (const gfft::Step& s : sl.steps)
         if (s.kind == gfft::Step::TC) ++info->tc_stages;
     for (const gfft::Step& s : sl.steps)
-        if (s.kind == gfft::Step::CLUSTER) info->cluster_ctas = s.cl.csize;
+        if (s.kind == gfft::Step::CLUSTER) {
+            info->cluster_ctas = s.cl.csize;
+            info->cluster_count = s.cl.clusters;
+        }
     for (const gfft::Step& s : sl.steps) {
         const gfft::InnerPlan* ip = nullptr;
         int tf = 0;
