@@ -271,7 +271,7 @@ struct ClusterArgs {
     float scale;
     int32_t smem_bytes;
     int32_t clusters;   // co-resident clusters (set when the plan is prepared on a device)
-    int32_t pad_;
+    int32_t length;     // transform length N = Q*P
 };
 
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with

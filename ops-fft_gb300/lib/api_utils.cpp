@@ -172,8 +172,7 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
         } else if (s.kind == gfft::Step::CLUSTER) {
             // column radices then row radices; threads = all CTAs of a cluster
             int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
-            const long long n = plan->rank == 2 ? 0 : (long long)plan->lengths[0];
-            if (gfft_cluster_lookup(n, s.cl.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) == s.cl.kid) {
+            if (gfft_cluster_lookup(s.cl.length, s.cl.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) == s.cl.kid) {
                 info->nradix = 4;
                 info->radix[0] = Q0;
                 info->radix[1] = Q / Q0;

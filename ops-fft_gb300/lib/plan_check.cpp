@@ -273,9 +273,10 @@ bool check_tc(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
 // Cluster transform: the configuration matches the length, every HBM
 // access of the column loads and row stores, the twiddle ranges and the
 // receive-buffer offsets of the distributed shared-memory stores.
-bool check_cluster(const Step& s, const Bufs& b, int64_t n, int64_t tw_count, std::string& why)
+bool check_cluster(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
 {
     const ClusterArgs& a = s.cl;
+    const int64_t n = a.length;
     int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
     if (gfft_cluster_lookup(n, a.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) != a.kid) return fail(why, "cluster config");
     if ((int64_t)Q * P != n || P % C || Q % C) return fail(why, "cluster split");
@@ -349,7 +350,7 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
             else if (s.kind == Step::COL) ok = check_col(s, b, impl->tb.count, why);
             else if (s.kind == Step::PACK) ok = check_pack(s, b, impl->tb.count, why);
             else if (s.kind == Step::TC) ok = check_tc(s, b, impl->tb.count, why);
-            else if (s.kind == Step::CLUSTER) ok = check_cluster(s, b, p.n0, impl->tb.count, why);
+            else if (s.kind == Step::CLUSTER) ok = check_cluster(s, b, impl->tb.count, why);
             else if (s.kind == Step::COPY)
                 ok = (s.copy_bytes <= b.bytes[s.src] && s.copy_bytes <= b.bytes[s.dst]) || fail(why, "copy size");
             if (!ok) {

@@ -565,6 +565,7 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st)
     a.scale = 1.f;
     a.smem_bytes = smem;
     a.clusters = 0;
+    a.length = (int32_t)n;
     st.tw_off = 0;
     return true;
 }
@@ -888,10 +889,17 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
         pk.pack.scale = 1.f;
         pk.post_off = tb.add_linear(L / 2 + 1, N, 1);
         bool spare = false;
+        Step cl;
+        const bool use_cluster = make_cluster_step(L, p.batch, tb, cl);
         if (r2c) {
             // input (float2 view) -> ... -> WS, then pack WS -> out
-            if (!make_axis_steps(L, 1, p.batch, L, IN, BUF_WS, BUF_WS2, cap, tb, out.steps, spare))
+            if (use_cluster) {
+                cl.src = IN;
+                cl.dst = BUF_WS;
+                out.steps.push_back(cl);
+            } else if (!make_axis_steps(L, 1, p.batch, L, IN, BUF_WS, BUF_WS2, cap, tb, out.steps, spare)) {
                 return unsupported("length not decomposable");
+            }
             pk.pack.in_dist = L;
             pk.pack.out_dist = nb;
             pk.src = BUF_WS;
@@ -903,9 +911,16 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
             pk.src = IN;
             pk.dst = BUF_WS;
             out.steps.push_back(pk);
-            if (!make_axis_steps(L, 1, p.batch, L, BUF_WS, BUF_OUT, BUF_WS2, cap, tb, out.steps, spare))
-                return unsupported("length not decomposable");
-            out.steps.back().col.conj_out = 1;
+            if (use_cluster) {
+                cl.src = BUF_WS;
+                cl.dst = BUF_OUT;
+                cl.cl.conj_out = 1;
+                out.steps.push_back(cl);
+            } else {
+                if (!make_axis_steps(L, 1, p.batch, L, BUF_WS, BUF_OUT, BUF_WS2, cap, tb, out.steps, spare))
+                    return unsupported("length not decomposable");
+                out.steps.back().col.conj_out = 1;
+            }
         }
         need_ws(L * p.batch * 8);
         if (spare) need_ws2(L * p.batch * 8);

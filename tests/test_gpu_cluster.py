@@ -92,3 +92,51 @@ def test_cluster_adjoint_matches_backward():
         torch.cuda.synchronize()
     e = O.errors(gt.cpu().numpy(), O.c2c(x, +1))
     assert e["rel_l2"] <= BOUND, e
+
+
+@pytest.mark.parametrize("n", [16384, 65536, 131072])
+def test_cluster_real_transforms_vs_fp64(n):
+    # even real lengths beyond one CTA: the half-length complex transform
+    # runs on a cluster, the even/odd packing in its own kernel
+    b = 9
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    X = np.empty((b, n // 2 + 1), np.complex64)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        assert p.info().cluster_ctas > 0 and p.info().nsteps == 2
+        p.exec_r2c(x, X)
+    e = O.errors(X, O.r2c(x))
+    assert e["rel_l2"] <= BOUND, e
+    Xc = (rng.standard_normal((b, n // 2 + 1)) + 1j * rng.standard_normal((b, n // 2 + 1))).astype(np.complex64)
+    y = np.empty((b, n), np.float32)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        assert p.info().cluster_ctas > 0
+        p.exec_c2r(Xc, y)
+    e = O.errors(y, O.c2r(Xc, n))
+    assert e["rel_l2"] <= BOUND, e
+
+
+def test_cluster_real_adjoints_vs_torch():
+    n, b = 32768, 2
+    nb = n // 2 + 1
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((b, n))
+    w = rng.uniform(0, 1, (b, nb))
+    xt = torch.tensor(x, dtype=torch.float64, requires_grad=True)
+    (torch.tensor(w) * torch.fft.rfft(xt).abs() ** 2).sum().backward()
+    Xbar = (2 * w * O.r2c(x)).astype(np.complex64)
+    out = np.empty((b, n), np.float32)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        assert p.info().cluster_ctas > 0
+        p.exec_r2c_adjoint(Xbar, out)
+    e = O.errors(out, xt.grad.numpy())
+    assert e["rel_l2"] <= 1e-5, e
+    X = rng.standard_normal((b, nb)) + 1j * rng.standard_normal((b, nb))
+    v = rng.standard_normal((b, n))
+    Xt = torch.tensor(X, dtype=torch.complex128, requires_grad=True)
+    (torch.tensor(v) * torch.fft.irfft(Xt, n=n) * n).sum().backward()
+    g = np.empty((b, nb), np.complex64)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.exec_c2r_adjoint(v.astype(np.float32), g)
+    e = O.errors(g, Xt.grad.numpy())
+    assert e["rel_l2"] <= 1e-5, e
