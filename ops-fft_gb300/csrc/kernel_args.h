@@ -264,6 +264,7 @@ struct ClusterArgs {
     int64_t twq_off;    // blob offset: column-phase second-pass table, W_Q^{k*r} at r*Q0 + k
     int64_t twp_off;    // blob offset: row-phase second-pass table, W_P^{k*r} at r*P0 + k
     int64_t outer_off;  // blob offset: W_N^e, e < N
+    int64_t post_off;   // real modes: blob offset of W_{2N}^i, i <= N
     int32_t kid;        // configuration id (csrc/cluster_list.h)
     int32_t csize;      // CTAs per cluster (must match the configuration)
     int32_t conj_in;
@@ -271,7 +272,10 @@ struct ClusterArgs {
     float scale;
     int32_t smem_bytes;
     int32_t clusters;   // co-resident clusters (set when the plan is prepared on a device)
-    int32_t length;     // transform length N = Q*P
+    int32_t length;     // complex transform length N = Q*P
+    int32_t io_mode;    // IO_C2C; IO_R2C_EVEN / IO_C2R_EVEN: real length 2N with fused packing
+    int32_t weight;     // WeightMode of the real modes
+    int32_t pad_;
 };
 
 // Twiddle table segment: out[i] = W_M^{f(i)} (forward sign) with
@@ -302,10 +306,10 @@ int gfft_launch_cluster(const gfft::ClusterArgs* a, void* stream);
 // (or -1) and fills the cluster size, the column/row lengths, their first
 // radices, the threads per CTA and the dynamic shared memory per CTA.  want_c > 0 selects that cluster size.
 int gfft_cluster_lookup(long long n, int want_c, int* csize, int* q, int* p, int* q0, int* p0, int* nt, int* smem_bytes);
-// Sets the kernel attributes of configuration kid on the current device and
+// Sets the kernel attributes of configuration kid (io mode `mode`) on the current device and
 // returns how many of its clusters are co-resident (negative CUDA error on
 // failure).  Not stream-ordered: call outside stream capture.
-int gfft_cluster_prepare(int kid);
+int gfft_cluster_prepare(int kid, int mode);
 // Prepares the ragged kernel for a shared-memory size (attributes) and
 // returns its resident CTAs per SM (0 on error).  Not stream-ordered: call
 // outside stream capture.

@@ -233,7 +233,7 @@ aclfftResult plan_device_setup(PlanImpl* p)
     for (StepList& sl : p->lists) {
         for (Step& s : sl.steps) {
             if (s.kind != Step::CLUSTER) continue;
-            const int n = gfft_cluster_prepare(s.cl.kid);
+            const int n = gfft_cluster_prepare(s.cl.kid, s.cl.io_mode);
             if (n < 1) {
                 cudaGetLastError();
                 plan_impl_free(p);

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "handle.h"
 
@@ -281,11 +282,34 @@ bool check_cluster(const Step& s, const Bufs& b, int64_t tw_count, std::string& 
     if (gfft_cluster_lookup(n, a.csize, &C, &Q, &P, &Q0, &P0, &nt, &smem) != a.kid) return fail(why, "cluster config");
     if ((int64_t)Q * P != n || P % C || Q % C) return fail(why, "cluster split");
     if (smem != a.smem_bytes || smem > kMaxSmemBytes) return fail(why, "cluster shared memory");
-    if (a.ntf < 1 || a.in_dist < n || a.out_dist < n) return fail(why, "cluster sizes");
+    if (a.io_mode != IO_C2C && a.io_mode != IO_R2C_EVEN && a.io_mode != IO_C2R_EVEN) return fail(why, "cluster mode");
+    // the real modes read (C2R) or write (R2C) bin n as well
+    const int64_t in_hi = a.io_mode == IO_C2R_EVEN ? n : n - 1;
+    const int64_t out_hi = a.io_mode == IO_R2C_EVEN ? n : n - 1;
+    if (a.ntf < 1 || a.in_dist <= in_hi || a.out_dist <= out_hi) return fail(why, "cluster sizes");
     const int64_t ein = b.bytes[s.src] / 8, eout = b.bytes[s.dst] / 8;
-    if ((a.ntf - 1) * a.in_dist + (int64_t)(Q - 1) * P + (P - 1) >= ein) return fail(why, "cluster load out of bounds");
-    if ((a.ntf - 1) * a.out_dist + (Q - 1) + (int64_t)Q * (P - 1) >= eout)
-        return fail(why, "cluster store out of bounds");
+    if ((a.ntf - 1) * a.in_dist + in_hi >= ein) return fail(why, "cluster load out of bounds");
+    if ((a.ntf - 1) * a.out_dist + out_hi >= eout) return fail(why, "cluster store out of bounds");
+    if (a.io_mode != IO_C2C && (a.post_off < 0 || a.post_off + n + 1 > tw_count))
+        return fail(why, "cluster packing twiddles out of table");
+    if (a.io_mode == IO_R2C_EVEN) {
+        // symmetric row ownership: every row k_q lands on exactly one CTA
+        // slot, and k_q and Q - k_q on the same CTA
+        const int H = Q / C / 2;
+        std::vector<int> seen((size_t)Q, 0);
+        for (int kq = 0; kq < Q; ++kq) {
+            int d, l;
+            if (kq == 0) { d = 0; l = 0; }
+            else if (kq == Q / 2) { d = 0; l = H; }
+            else if (kq < Q / 2) { d = kq / H; l = kq % H; }
+            else { d = (Q - kq) / H; l = H + (Q - kq) % H; }
+            if (d >= C || l >= Q / C) return fail(why, "cluster r2c row map");
+            if (seen[(size_t)(d * (Q / C) + l)]++) return fail(why, "cluster r2c row map not one-to-one");
+            const int m = (Q - kq) % Q;
+            const int dm = m == 0 ? 0 : (m == Q / 2 ? 0 : (m < Q / 2 ? m / H : (Q - m) / H));
+            if (dm != d) return fail(why, "cluster r2c mirror rows split");
+        }
+    }
     if (a.twq_off < 0 || a.twq_off + Q > tw_count || a.twp_off < 0 || a.twp_off + P > tw_count)
         return fail(why, "cluster pass tables out of table");
     if (a.outer_off < 0 || a.outer_off + n > tw_count) return fail(why, "cluster outer twiddles out of table");

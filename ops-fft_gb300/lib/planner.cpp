@@ -541,9 +541,12 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     return true;
 }
 
-// Whole batched C2C of length n on thread-block clusters (one cluster per
-// transform, see csrc/cluster_fft.cu).  False when no configuration exists.
-bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st)
+// Whole batched transform on thread-block clusters (one cluster per
+// transform, see csrc/cluster_fft.cuh): a C2C of length n (io_mode IO_C2C)
+// or an even R2C / C2R of real length 2n with the packing fused
+// (IO_R2C_EVEN / IO_C2R_EVEN).  False when no configuration exists.
+bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st, int io_mode = IO_C2C,
+                       int weight = WEIGHT_NONE)
 {
     if (!clusters_enabled() || n > 0x7fffffff) return false;
     const char* env_c = std::getenv("OPS_FFT_CLUSTER_C");
@@ -557,8 +560,12 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st)
     a.kid = kid;
     a.csize = C;
     a.ntf = batch;
-    a.in_dist = n;
-    a.out_dist = n;
+    a.in_dist = io_mode == IO_C2R_EVEN ? n + 1 : n;
+    a.out_dist = io_mode == IO_R2C_EVEN ? n + 1 : n;
+    a.io_mode = io_mode;
+    a.weight = weight;
+    a.conj_out = io_mode == IO_C2R_EVEN ? 1 : 0;
+    a.post_off = io_mode == IO_C2C ? 0 : tb.add_linear(n + 1, 2 * n, 1);
     a.twq_off = tb.add_pass_table(Q0, Q / Q0);
     a.twp_off = tb.add_pass_table(P0, P / P0);
     a.outer_off = tb.add_linear(n, n, 1);
@@ -878,6 +885,29 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
         if (L <= row_max_length() && row_feasible((int)L, mode)) {
             if (!single(mode, (int)L, r2c ? L : nb, r2c ? nb : L)) return false;
             return true;
+        }
+        // long real transforms on a cluster, packing fused (an in-place call
+        // first copies the input to the workspace: input and output rows
+        // have different pitches)
+        {
+            Step cl;
+            if (make_cluster_step(L, p.batch, tb, cl, mode, p.weight)) {
+                int src = IN;
+                if (inplace) {
+                    Step cp;
+                    cp.kind = Step::COPY;
+                    cp.copy_bytes = in_bytes;
+                    cp.src = BUF_OUT;
+                    cp.dst = BUF_WS;
+                    out.steps.push_back(cp);
+                    need_ws(in_bytes);
+                    src = BUF_WS;
+                }
+                cl.src = src;
+                cl.dst = BUF_OUT;
+                out.steps.push_back(cl);
+                return true;
+            }
         }
         // long real transforms: separate packing around a multi-pass C2C
         Step pk;

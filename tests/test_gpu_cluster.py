@@ -94,25 +94,59 @@ def test_cluster_adjoint_matches_backward():
     assert e["rel_l2"] <= BOUND, e
 
 
-@pytest.mark.parametrize("n", [16384, 65536, 131072])
-def test_cluster_real_transforms_vs_fp64(n):
+@pytest.mark.parametrize("n,c", [(16384, 4), (32768, 4), (32768, 8), (65536, 8), (131072, 16), (131072, 8)])
+def test_cluster_real_transforms_vs_fp64(n, c, monkeypatch):
     # even real lengths beyond one CTA: the half-length complex transform
-    # runs on a cluster, the even/odd packing in its own kernel
-    b = 9
-    rng = np.random.default_rng(n)
+    # runs on a cluster with the even/odd packing fused (one launch); the
+    # batch exceeds the co-resident clusters
+    monkeypatch.setenv("OPS_FFT_CLUSTER_C", str(c))
+    b = max(9, (1 << 24) // n)
+    rng = np.random.default_rng(n + c)
     x = rng.standard_normal((b, n)).astype(np.float32)
     X = np.empty((b, n // 2 + 1), np.complex64)
     with A.Plan.plan1d(n, A.R2C, b) as p:
-        assert p.info().cluster_ctas > 0 and p.info().nsteps == 2
+        assert p.info().cluster_ctas == c and p.info().nsteps == 1
         p.exec_r2c(x, X)
     e = O.errors(X, O.r2c(x))
     assert e["rel_l2"] <= BOUND, e
     Xc = (rng.standard_normal((b, n // 2 + 1)) + 1j * rng.standard_normal((b, n // 2 + 1))).astype(np.complex64)
     y = np.empty((b, n), np.float32)
     with A.Plan.plan1d(n, A.C2R, b) as p:
-        assert p.info().cluster_ctas > 0
+        assert p.info().cluster_ctas == c and p.info().nsteps == 1
         p.exec_c2r(Xc, y)
     e = O.errors(y, O.c2r(Xc, n))
+    assert e["rel_l2"] <= BOUND, e
+
+
+def test_cluster_real_inplace_scaled_and_impulses():
+    # in place (a copy step first), backward normalisation, and impulses
+    # whose exact spectra pin the post-process pairing of rows 0, Q/2 and
+    # the mirrored rows
+    n, b = 65536, 4
+    dev = torch.device("cuda:0")
+    x = np.zeros((b, n), np.float32)
+    x[0, 1] = 1.0
+    x[1, 3] = -2.0
+    x[2, n - 1] = 0.5
+    x[3] = np.random.default_rng(9).standard_normal(n)
+    nb = n // 2 + 1
+    buf = torch.zeros(b * nb * 2, dtype=torch.float32, device=dev)
+    buf[: b * n] = torch.from_numpy(x.reshape(-1)).to(dev)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        assert p.info().cluster_ctas > 0
+        p.set_stream(torch.cuda.current_stream(dev))
+        p.exec_r2c(buf, buf)
+        torch.cuda.synchronize()
+    X = buf.cpu().numpy().view(np.complex64).reshape(b, nb)
+    exact = O.r2c(x)
+    assert np.abs(X[:3] - exact[:3]).max() <= 1e-5
+    e = O.errors(X, exact)
+    assert e["rel_l2"] <= BOUND, e
+    y = np.empty((b, n), np.float32)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.set_norm(A.NORM_BACKWARD)
+        p.exec_c2r(X, y)
+    e = O.errors(y, x)
     assert e["rel_l2"] <= BOUND, e
 
 
