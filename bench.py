@@ -2,7 +2,7 @@
 """Benchmark of the batched FP32 transform path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5|long]
 
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
@@ -512,6 +512,117 @@ class Cfg5:
                                              inf.twiddle_entries * 8)}
 
 
+class LongWorkload:
+    """Large batched C2C and R2C at N = 4096, 16384, 65536 (the lengths of
+    the 70%-of-HBM target): 256 MB of complex input per C2C launch (128 MB
+    of real input per R2C launch), far above the L2, x ~ N(0,1).  One step
+    runs every (kind, N) once; each launch is timed with CUDA events so the
+    per-length roofline fractions are reported next to the aggregate."""
+
+    name = "long_c2c_r2c"
+    LENGTHS = (4096, 16384, 65536)
+    POINTS = 1 << 25  # complex points per C2C launch
+
+    def __init__(self, torch, A, dev, stream, nsets):
+        self.torch, self.A = torch, A
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        self.items = []  # (kind, n, batch, plan, bytes)
+        for n in self.LENGTHS:
+            b = self.POINTS // n
+            for kind in ("C2C", "R2C"):
+                p = A.Plan.plan1d(n, getattr(A, kind), b)
+                p.set_stream(stream)
+                byt = 16 * n * b if kind == "C2C" else b * (4 * n + 8 * (n // 2 + 1))
+                self.items.append((kind, n, b, p, byt))
+        self.sets = []
+        for _ in range(nsets):
+            s = {}
+            for kind, n, b, _, _ in self.items:
+                if kind == "C2C":
+                    x = torch.complex(torch.randn((b, n), generator=g), torch.randn((b, n), generator=g)).to(dev)
+                    y = torch.empty_like(x)
+                else:
+                    x = torch.randn((b, n), generator=g).to(dev)
+                    y = torch.empty((b, n // 2 + 1), dtype=torch.complex64, device=dev)
+                s[(kind, n)] = (x, y)
+            self.sets.append(s)
+        self.alg_bytes_per_step = sum(it[4] for it in self.items)
+        self.launches_per_step = sum(it[3].info().nsteps for it in self.items)
+        dom = max(self.items, key=lambda it: it[4] if it[0] == "C2C" and it[1] == 65536 else 0)
+        self.dom_key = (dom[0], dom[1])
+        self.dominant = (f"C2C N=65536 batch={dom[2]} (thread-block cluster, {dom[3].info().cluster_ctas} CTAs)",
+                         dom[4])
+        self.set_bytes = sum(x.numel() * x.element_size() + y.numel() * y.element_size()
+                             for x, y in self.sets[0].values())
+        self.per_item_ms = {}
+
+    def _run(self, kind, p, x, y):
+        if kind == "C2C":
+            p.exec_c2c(x, y, self.A.FORWARD)
+        else:
+            p.exec_r2c(x, y)
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        for kind, n, b, p, _ in self.items:
+            x, y = s[(kind, n)]
+            if dom_events is not None:
+                ev = self.item_events[(kind, n)]
+                e0 = self.torch.cuda.Event(enable_timing=True)
+                e1 = self.torch.cuda.Event(enable_timing=True)
+                e0.record()
+                self._run(kind, p, x, y)
+                e1.record()
+                ev.append((e0, e1))
+            else:
+                self._run(kind, p, x, y)
+
+    def reset_item_events(self):
+        self.item_events = {(it[0], it[1]): [] for it in self.items}
+
+    def item_times_ms(self):
+        return {k: statistics.mean(a.elapsed_time(b) for a, b in v) for k, v in self.item_events.items() if v}
+
+    def make_host(self):
+        torch = self.torch
+        self.host = {}
+        h2d = d2h = 0
+        for kind, n, b, _, _ in self.items:
+            x, y = self.sets[0][(kind, n)]
+            hx = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+            hx.copy_(x.cpu())
+            hy = torch.empty(y.shape, dtype=y.dtype, pin_memory=True)
+            self.host[(kind, n)] = (hx, hy)
+            h2d += hx.numel() * hx.element_size()
+            d2h += hy.numel() * hy.element_size()
+        return h2d, d2h
+
+    def step_host(self):
+        for kind, n, b, p, _ in self.items:
+            hx, hy = self.host[(kind, n)]
+            self._run(kind, p, hx, hy)
+
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        done = 0
+        t0 = time.perf_counter()
+        for n in self.LENGTHS:
+            r = max(1, rows * 4096 // n)
+            x = (rng.standard_normal((r, n)) + 1j * rng.standard_normal((r, n))).astype(np.complex64)
+            O.port_c2c(x, -1, nthreads)
+            xr = rng.standard_normal((r, n)).astype(np.float32)
+            O.port_r2c(xr, nthreads)
+            done += r * (16 * n + 4 * n + 8 * (n // 2 + 1))
+        return done, time.perf_counter() - t0
+
+    def config(self):
+        return {"workload": "large batched 1D C2C and R2C, N = 4096, 16384, 65536 (inputs far above L2)",
+                "sizes": [[kind, n, b] for kind, n, b, _, _ in self.items],
+                "dtype": "complex64 interleaved / float32 real"}
+
+
 def make_workload(name, torch, A, dev, stream, nsets):
     if name == "cfg2":
         return Cfg2(torch, A, dev, stream, nsets)
@@ -525,6 +636,8 @@ def make_workload(name, torch, A, dev, stream, nsets):
         return Cfg4(torch, A, dev, stream, nsets)
     if name == "cfg5":
         return Cfg5(torch, A, dev, stream, nsets)
+    if name == "long":
+        return LongWorkload(torch, A, dev, stream, nsets)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -597,6 +710,8 @@ def main():
         for i in range(args.warmup):
             wl.step(i)
         torch.cuda.synchronize()
+        if isinstance(wl, LongWorkload):
+            wl.reset_item_events()
         dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         if dist:
@@ -609,6 +724,8 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
+        if isinstance(wl, LongWorkload):
+            return t0.elapsed_time(t1), wl.item_times_ms()[wl.dom_key]
         return t0.elapsed_time(t1), statistics.mean(a.elapsed_time(b) for a, b in dom_ev)
 
     nk = args.steps
@@ -652,7 +769,7 @@ def main():
         for _ in range(2):
             wl.step_host()
         torch.cuda.synchronize()
-        ke = max(3, min(nk, 10))
+        ke = 3 if isinstance(wl, LongWorkload) else max(3, min(nk, 10))
         if dist:
             dist.barrier()
         ts = time.perf_counter()
@@ -678,6 +795,14 @@ def main():
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
         if isinstance(wl, (Cfg4, Cfg5)):
             cfg["fp64_error"] = wl.fp64_errors()
+        if isinstance(wl, LongWorkload):
+            per = {}
+            for (kind, n), t_ms in wl.item_times_ms().items():
+                byt = next(it[4] for it in wl.items if (it[0], it[1]) == (kind, n))
+                gbs = byt / (t_ms / 1e3) / 1e9
+                per[f"{kind} {n}"] = {"us": round(t_ms * 1e3, 1), "GB/s": round(gbs, 1),
+                                      "frac_of_measured_hbm": round(gbs / peak, 3)}
+            cfg["per_length"] = per
         if forms is not None:
             cfg["forms"] = forms
             cfg["fp64_reference"] = "torch.fft.fft in complex128 on the same device inputs"
@@ -715,6 +840,11 @@ def run_reference(args, rank, world):
         wl.batch = 4096
         cfg = Cfg2.config(wl)
         sample = lambda rows, th: Cfg2.cpu_sample(wl, O, rows, th)
+    elif wlname == "long":
+        wl = LongWorkload.__new__(LongWorkload)
+        wl.items = [(k, n, LongWorkload.POINTS // n, None, 0) for n in LongWorkload.LENGTHS for k in ("C2C", "R2C")]
+        cfg = LongWorkload.config(wl)
+        sample = lambda rows, th: LongWorkload.cpu_sample(wl, O, rows, th)
     else:
         wl = C2CWorkload.__new__(C2CWorkload)
         wl.sizes = [(4096, 256)] if wlname == "cfg1" else [(65536, 64), (16384, 64)]
