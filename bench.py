@@ -13,10 +13,12 @@ algorithmic bytes of the transforms only (one read of each transform's
 input + one write of its output) per second of the whole step.
 
 Timing: inputs resident in HBM, rotating buffer sets whose total exceeds
-2x the L2 size, W warm-up steps, K timed steps between barriers and device
-synchronisation, CUDA events on the launch stream, max over ranks.
-`roofline` times every launch of the dominant kernel (R2C, N=3000) with
-CUDA events on its stream; `e2e` repeats the step through the C ABI with
+2x the L2 size, W warm-up steps, then the K timed steps captured in one CUDA
+graph on the launch stream and replayed once between barriers and device
+synchronisation, timed with CUDA events on that stream, max over ranks.
+`roofline` times K launches of the dominant kernel (R2C, N=3000) over the
+same buffer sets the same way (one graph, one replay, CUDA events on the
+launch stream) and divides by K; `e2e` repeats the step through the C ABI with
 host (pinned) buffers, so the host<->device copies are inside the timing;
 `cpu_baseline` times the FP32 port of the reference's CPU-side algorithm
 (oracle port) on a bounded sample of the same workload.
@@ -166,6 +168,10 @@ class Cfg2:
             self.torch.mul(b["X"], b["w2"], out=b["G"])
             pr.exec_r2c_adjoint(b["G"], b["gx"])
 
+    def dom_call(self, i):
+        b = self.sets[i % len(self.sets)][3000]
+        self.plans[3000][0].exec_r2c(b["x"], b["X"])
+
     # host-buffer variant through the same C ABI (the reference's calling
     # convention: host pointers in and out, return means done)
     def make_host(self):
@@ -288,6 +294,10 @@ class C2CWorkload:
             else:
                 self.plans[n].exec_c2c(s[n]["x"], s[n]["y"], self.A.FORWARD)
 
+    def dom_call(self, i):
+        s = self.sets[i % len(self.sets)][self.dom_n]
+        self.plans[self.dom_n].exec_c2c(s["x"], s["y"], self.A.FORWARD)
+
     def make_host(self):
         torch = self.torch
         self.host = {}
@@ -356,6 +366,10 @@ class Cfg4:
             dom_events[1].record()
         self.pi.exec_c2c(s["Y"], s["Z"], self.A.BACKWARD)
         self.pf.exec_c2c_adjoint(s["G"], s["gx"], self.A.FORWARD)
+
+    def dom_call(self, i):
+        s = self.sets[i % len(self.sets)]
+        self.pf.exec_c2c(s["x"], s["Y"], self.A.FORWARD)
 
     def make_host(self):
         torch = self.torch
@@ -439,6 +453,10 @@ class Cfg5:
         self.plan.exec(s["x"], s["y"], self.A.FORWARD)
         if dom_events is not None:
             dom_events[1].record()
+
+    def dom_call(self, i):
+        s = self.sets[i % len(self.sets)]
+        self.plan.exec(s["x"], s["y"], self.A.FORWARD)
 
     def make_host(self):
         torch = self.torch
@@ -577,6 +595,14 @@ class LongWorkload:
             else:
                 self._run(kind, p, x, y)
 
+    def item_call(self, key, i):
+        it = next(it for it in self.items if (it[0], it[1]) == key)
+        x, y = self.sets[i % len(self.sets)][key]
+        self._run(it[0], it[3], x, y)
+
+    def dom_call(self, i):
+        self.item_call(self.dom_key, i)
+
     def reset_item_events(self):
         self.item_events = {(it[0], it[1]): [] for it in self.items}
 
@@ -698,18 +724,47 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    stream = torch.cuda.current_stream()
+    # all work runs on one non-default stream (the plans launch there, torch's
+    # elementwise kernels too), so the timed steps can be captured in a CUDA graph
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     l2 = torch.cuda.get_device_properties(dev).L2_cache_size
     probe = make_workload(args.workload, torch, A, dev, stream, 1)
     nsets = max(1, -(-2 * l2 // max(probe.set_bytes, 1)) + (1 if probe.set_bytes < 4 * l2 else 0))
     del probe
     torch.cuda.empty_cache()
     wl = make_workload(args.workload, torch, A, dev, stream, nsets)
+    timing_mode = []
 
-    def timed(nk):
-        for i in range(args.warmup):
-            wl.step(i)
+    def graph_ms(fn, nk):
+        """fn(0), ..., fn(nk-1) captured in ONE CUDA graph on the work stream,
+        replayed once untimed, then one replay timed with CUDA events on that
+        stream (barrier + synchronize on both sides).  None if capture fails."""
+        g = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(g, stream=stream):
+                for i in range(nk):
+                    fn(i)
+        except Exception as e:  # noqa: BLE001 - report and time eagerly instead
+            timing_mode.append(f"graph capture failed ({type(e).__name__}: {str(e)[:120]}), eager launches")
+            torch.cuda.synchronize()
+            return None
+        g.replay()
         torch.cuda.synchronize()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0.record(stream)
+        g.replay()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        del g
+        return t0.elapsed_time(t1)
+
+    def eager(nk):
         if isinstance(wl, LongWorkload):
             wl.reset_item_events()
         dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
@@ -725,8 +780,32 @@ def main():
         if dist:
             dist.barrier()
         if isinstance(wl, LongWorkload):
-            return t0.elapsed_time(t1), wl.item_times_ms()[wl.dom_key]
-        return t0.elapsed_time(t1), statistics.mean(a.elapsed_time(b) for a, b in dom_ev)
+            per = wl.item_times_ms()
+            return t0.elapsed_time(t1), per[wl.dom_key], per
+        return t0.elapsed_time(t1), statistics.mean(a.elapsed_time(b) for a, b in dom_ev), None
+
+    def timed(nk):
+        """(ms for nk steps, ms per dominant launch, per-item ms or None).
+        Steps: one graph of nk steps.  Dominant launch: one graph of nk
+        launches of that transform over the same rotating buffer sets."""
+        for i in range(args.warmup):
+            wl.step(i)
+        torch.cuda.synchronize()
+        ms = graph_ms(wl.step, nk)
+        if ms is None:
+            return eager(nk)
+        if isinstance(wl, LongWorkload):
+            per = {}
+            for key in [(it[0], it[1]) for it in wl.items]:
+                t = graph_ms(lambda i, k=key: wl.item_call(k, i), nk)
+                if t is None:
+                    return eager(nk)
+                per[key] = t / nk
+            return ms, per[wl.dom_key], per
+        t = graph_ms(wl.dom_call, nk)
+        if t is None:
+            return eager(nk)
+        return ms, t / nk, None
 
     nk = args.steps
     forms = None
@@ -737,7 +816,7 @@ def main():
         own = wl.prec
         for prec in (A.PREC_FP32, A.PREC_BF16X3, A.PREC_TF32X3):
             wl.set_prec(prec)
-            f_ms, f_dom = timed(nk)
+            f_ms, f_dom, _ = timed(nk)
             forms[wl.FORM_NAMES[prec]] = {
                 "GB/s": round(wl.alg_bytes_per_step * nk / (f_ms / 1e3) / 1e9, 1),
                 "dominant_us": round(f_dom * 1e3, 2), "launches_per_step": wl.launches_per_step,
@@ -746,7 +825,7 @@ def main():
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     time.sleep(0.3)
-    ms, dom_ms = timed(nk)
+    ms, dom_ms, per_item = timed(nk)
     clk = clocks.stop()
     if dist:
         tt = torch.tensor([ms], device=dev)
@@ -793,11 +872,14 @@ def main():
         cfg = wl.config()
         cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
+        cfg["timing"] = (timing_mode[-1] if timing_mode else
+                         f"one CUDA graph of {nk} steps (and one of {nk} dominant launches), one replay each timed "
+                         f"with CUDA events on the launch stream")
         if isinstance(wl, (Cfg4, Cfg5)):
             cfg["fp64_error"] = wl.fp64_errors()
         if isinstance(wl, LongWorkload):
             per = {}
-            for (kind, n), t_ms in wl.item_times_ms().items():
+            for (kind, n), t_ms in per_item.items():
                 byt = next(it[4] for it in wl.items if (it[0], it[1]) == (kind, n))
                 gbs = byt / (t_ms / 1e3) / 1e9
                 per[f"{kind} {n}"] = {"us": round(t_ms * 1e3, 1), "GB/s": round(gbs, 1),

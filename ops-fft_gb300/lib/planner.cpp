@@ -577,6 +577,17 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st, i
     return true;
 }
 
+// Lengths that a row kernel holds in one thread group (n <= 4096) run on a
+// cluster only when the batch is too small to fill the GPU with one group
+// per transform (at most OPS_FFT_CLUSTER_MAXBATCH transforms, default 1024);
+// longer lengths always prefer a cluster.
+bool cluster_for_batch(int64_t n, int64_t batch)
+{
+    if (n > 4096) return true;
+    const char* v = std::getenv("OPS_FFT_CLUSTER_MAXBATCH");
+    return batch <= (v ? (int64_t)std::atoll(v) : (int64_t)1024);
+}
+
 // Strided-axis transform as a list of column passes with buffer routing.
 bool make_axis_steps(int64_t n, int64_t S, int64_t items, int64_t D, int src, int dst, int spare, int cap,
                      TwiddleBuilder& tb, std::vector<Step>& out, bool& needs_spare)
@@ -831,7 +842,7 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
             if (spare) need_ws(N * p.stride * 8);
             return true;
         }
-        {
+        if (cluster_for_batch(N, p.batch)) {
             Step st;
             if (make_cluster_step(N, p.batch, tb, st)) {
                 st.src = IN;
@@ -882,16 +893,17 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
     if (N % 2 == 0) {
         const int64_t L = N / 2;
         const int mode = r2c ? IO_R2C_EVEN : IO_C2R_EVEN;
-        if (L <= row_max_length() && row_feasible((int)L, mode)) {
+        const bool row_ok = L <= row_max_length() && row_feasible((int)L, mode);
+        if (row_ok && !cluster_for_batch(L, p.batch)) {
             if (!single(mode, (int)L, r2c ? L : nb, r2c ? nb : L)) return false;
             return true;
         }
-        // long real transforms on a cluster, packing fused (an in-place call
-        // first copies the input to the workspace: input and output rows
-        // have different pitches)
+        // long real transforms (and short ones in small batches) on a
+        // cluster, packing fused (an in-place call first copies the input to
+        // the workspace: input and output rows have different pitches)
         {
             Step cl;
-            if (make_cluster_step(L, p.batch, tb, cl, mode, p.weight)) {
+            if (cluster_for_batch(L, p.batch) && make_cluster_step(L, p.batch, tb, cl, mode, p.weight)) {
                 int src = IN;
                 if (inplace) {
                     Step cp;
@@ -909,6 +921,7 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
                 return true;
             }
         }
+        if (row_ok) return single(mode, (int)L, r2c ? L : nb, r2c ? nb : L);
         // long real transforms: separate packing around a multi-pass C2C
         Step pk;
         pk.kind = Step::PACK;

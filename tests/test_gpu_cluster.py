@@ -20,7 +20,7 @@ torch = pytest.importorskip("torch")
 
 BOUND = 1e-6
 # (length, cluster size, batch)
-CASES = [(8192, 4, 301), (16384, 4, 150), (16384, 8, 77), (32768, 8, 60), (65536, 16, 40), (65536, 8, 37)]
+CASES = [(4096, 4, 301), (4096, 8, 203), (8192, 4, 301), (16384, 4, 150), (16384, 8, 77), (32768, 8, 60), (65536, 16, 40), (65536, 8, 37)]
 
 
 def _data(n, b, seed):
@@ -94,13 +94,14 @@ def test_cluster_adjoint_matches_backward():
     assert e["rel_l2"] <= BOUND, e
 
 
-@pytest.mark.parametrize("n,c", [(16384, 4), (32768, 4), (32768, 8), (65536, 8), (131072, 16), (131072, 8)])
+@pytest.mark.parametrize("n,c", [(8192, 4), (8192, 8), (16384, 4), (32768, 4), (32768, 8), (65536, 8), (131072, 16),
+                                 (131072, 8)])
 def test_cluster_real_transforms_vs_fp64(n, c, monkeypatch):
-    # even real lengths beyond one CTA: the half-length complex transform
-    # runs on a cluster with the even/odd packing fused (one launch); the
-    # batch exceeds the co-resident clusters
+    # even real lengths beyond one CTA (and N = 8192 in a small batch): the
+    # half-length complex transform runs on a cluster with the even/odd
+    # packing fused (one launch); the batch exceeds the co-resident clusters
     monkeypatch.setenv("OPS_FFT_CLUSTER_C", str(c))
-    b = max(9, (1 << 24) // n)
+    b = max(9, (1 << 24) // n) if n > 8192 else 700
     rng = np.random.default_rng(n + c)
     x = rng.standard_normal((b, n)).astype(np.float32)
     X = np.empty((b, n // 2 + 1), np.complex64)
@@ -174,3 +175,30 @@ def test_cluster_real_adjoints_vs_torch():
         p.exec_c2r_adjoint(v.astype(np.float32), g)
     e = O.errors(g, Xt.grad.numpy())
     assert e["rel_l2"] <= 1e-5, e
+
+
+def test_short_lengths_use_clusters_only_in_small_batches(monkeypatch):
+    # N = 4096 C2C and N = 8192 R2C: a cluster per transform for small
+    # batches, the one-group-per-transform row kernel above the batch limit;
+    # both give the FP64 result
+    for kind, n, b, lim, want in [(A.C2C, 4096, 256, None, True), (A.C2C, 4096, 256, "100", False),
+                                  (A.R2C, 8192, 64, None, True), (A.R2C, 8192, 64, "32", False)]:
+        if lim is None:
+            monkeypatch.delenv("OPS_FFT_CLUSTER_MAXBATCH", raising=False)
+        else:
+            monkeypatch.setenv("OPS_FFT_CLUSTER_MAXBATCH", lim)
+        rng = np.random.default_rng(n + b)
+        if kind == A.C2C:
+            x = _data(n, b, n + b)
+            y, info = _run(x, n, b)
+            ref = O.c2c(x, -1)
+        else:
+            x = rng.standard_normal((b, n)).astype(np.float32)
+            y = np.empty((b, n // 2 + 1), np.complex64)
+            with A.Plan.plan1d(n, A.R2C, b) as p:
+                info = p.info()
+                p.exec_r2c(x, y)
+            ref = O.r2c(x)
+        assert (info.cluster_ctas > 0) == want
+        e = O.errors(y, ref)
+        assert e["rel_l2"] <= BOUND, e
