@@ -12,8 +12,8 @@
     X(0, 65536, 16, 256, 256, 256, 2, 16, 16, 16, 16)     \
     X(1, 65536, 8, 256, 256, 512, 1, 16, 16, 16, 16)      \
     X(2, 32768, 8, 128, 256, 256, 2, 16, 8, 16, 16)       \
-    X(3, 16384, 4, 128, 128, 256, 2, 16, 8, 16, 8)        \
-    X(4, 16384, 8, 128, 128, 128, 3, 16, 8, 16, 8)        \
+    X(3, 16384, 8, 128, 128, 128, 3, 16, 8, 16, 8)        \
+    X(4, 16384, 4, 128, 128, 256, 2, 16, 8, 16, 8)        \
     X(5, 8192, 4, 64, 128, 128, 3, 8, 8, 16, 8)         \
     X(6, 4096, 4, 64, 64, 128, 5, 8, 8, 8, 8)           \
     X(7, 4096, 8, 64, 64, 64, 8, 8, 8, 8, 8)

@@ -55,6 +55,8 @@ struct CSpec {
         return e;
     }
     static constexpr int E = emax();
+    // transform groups a CTA can hold (launch bound / group size, at most 15)
+    static constexpr int NGMAX = (MAXT_ / NTHR_) < 15 ? (MAXT_ / NTHR_) : 15;
     static constexpr int PSHIFT = (R[0] % 2 == 0) ? 4 : 30;
     __host__ __device__ static constexpr int product()
     {
@@ -64,6 +66,7 @@ struct CSpec {
     }
     static_assert(product() == L, "radix product must equal L");
     static_assert(NTHR % 32 == 0, "transform groups are whole warps");
+    static_assert(NGMAX >= 1, "launch bound below one transform group");
 };
 
 template <class S>
@@ -76,9 +79,29 @@ __device__ __forceinline__ int cpad(int i)
     }
 }
 
-__device__ __forceinline__ void group_sync(int id, int nthreads)
+// bar.sync of transform group barrier `id` (1 .. NG) with an immediate
+// barrier operand, selected by a uniform branch.  With a register operand
+// ptxas reserves all 16 hardware barriers of the CTA, and ncu's occupancy
+// limit for 3 barriers per CTA is 21 CTAs per SM (a pool of ~64), so 16
+// barriers alone cap residency at 4 CTAs per SM; immediates reserve NG + 1.
+template <int NT, int I, int NG>
+__device__ __forceinline__ void bar_sync_id(int id)
 {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+    if constexpr (I >= NG) {
+        asm volatile("bar.sync %0, %1;" ::"n"(NG), "n"(NT) : "memory");
+    } else {
+        if (id == I) {
+            asm volatile("bar.sync %0, %1;" ::"n"(I), "n"(NT) : "memory");
+        } else {
+            bar_sync_id<NT, I + 1, NG>(id);
+        }
+    }
+}
+
+template <class S>
+__device__ __forceinline__ void group_sync(int id)
+{
+    bar_sync_id<S::NTHR, 1, S::NGMAX>(id);
 }
 
 // One in-place pass P of codelet S on the transform held in W (shared) or,
@@ -117,7 +140,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
         } else {
             load_all([&](int i) { return c.st2[i]; });
         }
-        group_sync(bar_id, S::NTHR);  // the raw row and the padded work layout share the slot
+        group_sync<S>(bar_id);  // the raw row and the padded work layout share the slot
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -129,7 +152,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
                 });
             }
         });
-        group_sync(bar_id, S::NTHR);  // in place: every read of this pass precedes any write
+        group_sync<S>(bar_id);  // in place: every read of this pass precedes any write
     }
     // ---- twiddle + butterfly
     sfor<NB>([&](auto bb) {
@@ -189,7 +212,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
                 });
             }
         });
-        group_sync(bar_id, S::NTHR);
+        group_sync<S>(bar_id);
     }
 }
 
@@ -277,7 +300,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             if (!mbar_wait_bounded(&bars[s], (phase >> s) & 1u)) flags[0] = 1;
             phase ^= 1u << s;
         }
-        group_sync(bar_id, S::NTHR);
+        group_sync<S>(bar_id);
         if (flags[0]) {
             if (leader) {
                 atomicOr(A.err, 1);
@@ -294,7 +317,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         if (flags[1 + s]) {
             const float* gs = reinterpret_cast<const float*>(src);
             for (int64_t i = tid; i < row_bytes / 4; i += S::NTHR) reinterpret_cast<float*>(row)[i] = __ldg(gs + i);
-            group_sync(bar_id, S::NTHR);
+            group_sync<S>(bar_id);
         }
         // work layout (padded, 16-byte aligned) overlaps the raw row: every
         // pass reads all its inputs before it writes
@@ -336,7 +359,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     pb[q] = c.st2[L - k];
                 }
             });
-            group_sync(bar_id, S::NTHR);
+            group_sync<S>(bar_id);
             sfor<NPP>([&](auto qq) {
                 constexpr int q = decltype(qq)::value;
                 const int k = tid + q * S::NTHR;
@@ -357,7 +380,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
                 }
             });
-            group_sync(bar_id, S::NTHR);
+            group_sync<S>(bar_id);
             from_slot = false;
         }
         codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off, from_slot, last_global, bar_id);
@@ -386,7 +409,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
                 }
             }
-            group_sync(bar_id, S::NTHR);
+            group_sync<S>(bar_id);
         }
         // the slot is free: refill it with the transform NST iterations ahead
         if (leader) {

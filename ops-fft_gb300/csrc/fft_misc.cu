@@ -84,14 +84,10 @@ extern "C" int gfft_launch_row(const RowArgs* a, void* stream)
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (a->codelet) {
     case -1: break;
-    case 0: return launch_codelet_0(a, st);
-    case 1: return launch_codelet_1(a, st);
-    case 2: return launch_codelet_2(a, st);
-    case 3: return launch_codelet_3(a, st);
-    case 4: return launch_codelet_4(a, st);
-    case 5: return launch_codelet_5(a, st);
-    case 6: return launch_codelet_6(a, st);
-    case 7: return launch_codelet_7(a, st);
+#define GFFT_CASE_ROW(ID, ...) \
+    case ID: return launch_codelet_##ID(a, st);
+        GFFT_CODELETS(GFFT_CASE_ROW)
+#undef GFFT_CASE_ROW
     default: return (int)cudaErrorInvalidValue;
     }
     switch (a->ip.rmax) {
@@ -106,14 +102,10 @@ extern "C" int gfft_launch_col(const ColArgs* a, void* stream)
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (a->codelet) {
     case -1: break;
-    case 0: return launch_coltile_0(a, st);
-    case 1: return launch_coltile_1(a, st);
-    case 2: return launch_coltile_2(a, st);
-    case 3: return launch_coltile_3(a, st);
-    case 4: return launch_coltile_4(a, st);
-    case 5: return launch_coltile_5(a, st);
-    case 6: return launch_coltile_6(a, st);
-    case 7: return launch_coltile_7(a, st);
+#define GFFT_CASE_COL(ID, ...) \
+    case ID: return launch_coltile_##ID(a, st);
+        GFFT_CODELETS(GFFT_CASE_COL)
+#undef GFFT_CASE_COL
     default: return (int)cudaErrorInvalidValue;
     }
     switch (a->ip.rmax) {
@@ -161,6 +153,34 @@ extern "C" int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix)
 {
     int maxt = 0;
     return gfft_codelet_lookup2(L, nthr, radices, nradix, &maxt);
+}
+
+extern "C" int gfft_codelet_find(int L, int variant)
+{
+    int k = 0;
+#define GFFT_FIND(ID, MT, MB, LL, NT, ...) \
+    if (L == LL && k++ == variant) return ID;
+    GFFT_CODELETS(GFFT_FIND)
+#undef GFFT_FIND
+    return -1;
+}
+
+extern "C" int gfft_codelet_info(int id, int* L, int* nthr, int* radices, int* nradix, int* maxt, int* minb)
+{
+#define GFFT_INFO(ID, MT, MB, LL, NT, ...)                     \
+    if (id == ID) {                                            \
+        const int r[] = {__VA_ARGS__};                         \
+        *L = LL;                                               \
+        *nthr = NT;                                            \
+        *maxt = MT;                                            \
+        *minb = MB;                                            \
+        *nradix = (int)(sizeof(r) / sizeof(r[0]));             \
+        for (int i = 0; i < *nradix; ++i) radices[i] = r[i];   \
+        return 0;                                              \
+    }
+    GFFT_CODELETS(GFFT_INFO)
+#undef GFFT_INFO
+    return -1;
 }
 
 extern "C" int gfft_codelet_lookup2(int L, int* nthr, int* radices, int* nradix, int* maxt)

@@ -323,4 +323,10 @@ int gfft_kernel_max_threads(int rmax);
 // and fills its thread count per transform and radix sequence.
 int gfft_codelet_lookup(int L, int* nthr, int* radices, int* nradix);
 int gfft_codelet_lookup2(int L, int* nthr, int* radices, int* nradix, int* max_threads_per_cta);
+// id of the k-th codelet_list.h entry of length L (-1 if none)
+int gfft_codelet_find(int L, int variant);
+// the compile-time spec of codelet `id`: length, threads per transform,
+// radices, launch bound (threads per CTA, CTAs per SM); -1 if no such id
+int gfft_codelet_info(int id, int* L, int* nthr, int* radices, int* nradix, int* max_threads_per_cta,
+                      int* min_ctas_per_sm);
 }

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "codelet.cuh"
+#include "codelet_list.h"
 #include "row_pipe.cuh"
 #include "stockham.cuh"
 
@@ -134,22 +135,11 @@ int launch_coltile_t(const ColArgs* a, cudaStream_t st)
     return (int)cudaGetLastError();
 }
 
-int launch_coltile_0(const ColArgs* a, cudaStream_t st);
-int launch_coltile_1(const ColArgs* a, cudaStream_t st);
-int launch_coltile_2(const ColArgs* a, cudaStream_t st);
-int launch_coltile_3(const ColArgs* a, cudaStream_t st);
-int launch_coltile_4(const ColArgs* a, cudaStream_t st);
-int launch_coltile_5(const ColArgs* a, cudaStream_t st);
-int launch_coltile_6(const ColArgs* a, cudaStream_t st);
-int launch_coltile_7(const ColArgs* a, cudaStream_t st);
-int launch_codelet_0(const RowArgs* a, cudaStream_t st);
-int launch_codelet_1(const RowArgs* a, cudaStream_t st);
-int launch_codelet_2(const RowArgs* a, cudaStream_t st);
-int launch_codelet_3(const RowArgs* a, cudaStream_t st);
-int launch_codelet_4(const RowArgs* a, cudaStream_t st);
-int launch_codelet_5(const RowArgs* a, cudaStream_t st);
-int launch_codelet_6(const RowArgs* a, cudaStream_t st);
-int launch_codelet_7(const RowArgs* a, cudaStream_t st);
+#define GFFT_DECL_LAUNCH(ID, ...)                           \
+    int launch_codelet_##ID(const RowArgs* a, cudaStream_t st); \
+    int launch_coltile_##ID(const ColArgs* a, cudaStream_t st);
+GFFT_CODELETS(GFFT_DECL_LAUNCH)
+#undef GFFT_DECL_LAUNCH
 int launch_row_r16(const RowArgs* a, cudaStream_t st);
 int launch_row_r47(const RowArgs* a, cudaStream_t st);
 int launch_col_r16(const ColArgs* a, cudaStream_t st);

@@ -79,8 +79,9 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     if (a.tfpc < 1) return fail(why, "row tile");
     if (a.nstage < 1 || a.nstage > 4) return fail(why, "row stages");
     if (a.codelet >= 0) {
-        int cn = 0, cr[kMaxPass], cnr = 0;
-        if (gfft_codelet_lookup(L, &cn, cr, &cnr) != a.codelet || cn != a.ip.nthr || cnr != a.ip.npass)
+        int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+        if (gfft_codelet_info(a.codelet, &cl, &cn, cr, &cnr, &cmaxt, &cminb) != 0 || cl != L || cn != a.ip.nthr ||
+            cnr != a.ip.npass)
             return fail(why, "codelet mismatch");
         for (int p = 0; p < cnr; ++p)
             if (cr[p] != a.ip.pass[p].radix) return fail(why, "codelet radix mismatch");
@@ -100,8 +101,8 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
         const int64_t slots_end = 64 + (int64_t)a.nstage * a.stage_bytes;
         if (a.stage_bytes < a.in_dist * a.in_esize + 32 || a.stage_bytes < 16 + (int64_t)a.lpad * 8 || a.tfpc != 1)
             return fail(why, "codelet slot too small");
-        int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
-        gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt);
+        int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+        gfft_codelet_info(a.codelet, &cl, &cn, cr, &cnr, &cmaxt, &cminb);
         if (a.ngroups < 1 || a.ngroups > 15 || a.ngroups * a.ip.nthr > cmaxt) return fail(why, "codelet groups");
         if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
             a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 128 || a.group_bytes % 128 ||

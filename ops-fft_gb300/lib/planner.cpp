@@ -208,9 +208,14 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
                        TwiddleBuilder& tb, Step& st)
 {
     if (!codelets_enabled()) return false;
-    int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
-    const int id = gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt);
+    // OPS_FFT_CODELET_VARIANT=k selects the k-th entry of this length
+    // (tuning experiments); unset or absent, the first one
+    const char* env_var = std::getenv("OPS_FFT_CODELET_VARIANT");
+    int id = gfft_codelet_find(L, env_var ? std::atoi(env_var) : 0);
+    if (id < 0) id = gfft_codelet_find(L, 0);
     if (id < 0) return false;
+    int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+    if (gfft_codelet_info(id, &cl, &cn, cr, &cnr, &cmaxt, &cminb) != 0 || cl != L) return false;
     const std::vector<int> rad(cr, cr + cnr);
     const bool even_mode = io_mode == IO_R2C_EVEN || io_mode == IO_C2R_EVEN;
     const bool staged = false;
@@ -266,7 +271,7 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
             // registers: the launch bound caps each thread at 65536 / (MAXT * MINB);
             // they are allocated per warp in each of the 4 SM sub-partitions
             // (16384 registers each), so resident warps come in multiples of 4
-            const int64_t reg_cap = cmaxt <= 384 ? 80 : 128;
+            const int64_t reg_cap = std::min<int64_t>(255, (65536 / ((int64_t)cmaxt * cminb)) & ~(int64_t)7);
             const int64_t warps_by_regs = 4 * (16384 / (reg_cap * 32));
             const int64_t ctas = std::min<int64_t>(
                 {(228 * 1024) / (smem + 1024), 64 / warps, 32, warps_by_regs / warps});

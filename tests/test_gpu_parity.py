@@ -160,8 +160,12 @@ def test_config1_c2c_4096x256_device():
         assert np.array_equal(xd.cpu().numpy(), y)
 
 
-@pytest.mark.parametrize("n", [3000, 1024])
-def test_config2_r2c_c2r_batch4096_device(n):
+@pytest.mark.parametrize("n,variant", [(3000, None), (1024, None), (3000, "1"), (1024, "1")])
+def test_config2_r2c_c2r_batch4096_device(n, variant, monkeypatch):
+    # variant "1": the second codelet of the length (a 64-register build of
+    # the same radix sequence), selected by OPS_FFT_CODELET_VARIANT
+    if variant is not None:
+        monkeypatch.setenv("OPS_FFT_CODELET_VARIANT", variant)
     g = torch.Generator().manual_seed(12345)
     b = 4096
     x = torch.randn((b, n), generator=g)
