@@ -479,10 +479,21 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) coltile_kernel(const __grid_
         float2* ob = gout + item * A.out_dist + (j / A.out_split) * A.out_hi + (j % A.out_split) * A.out_lo;
         float2* Wc = tile + (int64_t)cc * A.wsize;
         if (ok) {
-            for (int r = r0; r < L; r += rstep) {
-                float2 x = ldg2(ib + (int64_t)r * A.in_stride);
-                if (A.conj_in) x.y = -x.y;
-                Wc[cpad<S>(r)] = x;
+            // batches of 8 independent loads per thread keep enough bytes in
+            // flight for the strided rows (one load at a time leaves the SM
+            // waiting on HBM latency)
+            for (int r = r0; r < L; r += 8 * rstep) {
+                float2 x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int rr = r + u * rstep;
+                    x[u] = rr < L ? ldg2(ib + (int64_t)rr * A.in_stride) : make_float2(0.f, 0.f);
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const int rr = r + u * rstep;
+                    if (rr < L) Wc[cpad<S>(rr)] = A.conj_in ? cconj(x[u]) : x[u];
+                }
             }
         }
         __syncthreads();

@@ -3,7 +3,8 @@
 // with MINB CTAs per SM (register cap 65536 / (MAXT * MINB)); the planner
 // picks the first entry whose length matches exactly, or the k-th one with
 // OPS_FFT_CODELET_VARIANT=k (entries after the first for a length are
-// variants: other register caps or radix orders).  Each entry is
+// variants: other register caps or radix orders; a column pass takes the
+// first entry of its length whose launch bound holds 8 columns).  Each entry is
 // instantiated in its own translation unit (codelet_<id>.cu) so the build
 // runs in parallel.
 #pragma once
@@ -17,5 +18,6 @@
     X(6, 384, 2, 128, 32, 8, 16)               \
     X(7, 512, 1, 8192, 512, 16, 16, 16, 2)     \
     X(8, 160, 6, 1500, 160, 15, 10, 10)        \
-    X(9, 128, 8, 512, 64, 8, 8, 8)
-#define GFFT_NUM_CODELETS 10
+    X(9, 128, 8, 512, 64, 8, 8, 8)             \
+    X(10, 1024, 1, 2048, 128, 16, 16, 8)
+#define GFFT_NUM_CODELETS 11

@@ -159,8 +159,9 @@ bool check_col(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const int L = a.ip.L;
     if (a.codelet >= 0) {
         // column-tile codelet: the codelet's compile-time spec must match the plan
-        int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
-        if (gfft_codelet_lookup2(L, &cn, cr, &cnr, &cmaxt) != a.codelet) return fail(why, "coltile codelet id");
+        int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+        if (gfft_codelet_info(a.codelet, &cl, &cn, cr, &cnr, &cmaxt, &cminb) != 0 || cl != L)
+            return fail(why, "coltile codelet id");
         if (cn != a.ip.nthr || cnr != a.ip.npass) return fail(why, "coltile spec");
         for (int q = 0; q < cnr; ++q)
             if (cr[q] != a.ip.pass[q].radix) return fail(why, "coltile radices");

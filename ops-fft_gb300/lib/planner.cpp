@@ -494,8 +494,13 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     // plain column passes of a length with a codelet run as column tiles of
     // that codelet (one transform group per column, in-place passes)
     if (Ns == 1 && !staged_out && codelets_enabled()) {
-        int cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0;
-        const int id = gfft_codelet_lookup2(Lq, &cn, cr, &cnr, &cmaxt);
+        // the first codelet of this length whose launch bound holds 8 columns
+        int id = -1, cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+        for (int k = 0; id < 0; ++k) {
+            const int cand = gfft_codelet_find(Lq, k);
+            if (cand < 0) break;
+            if (gfft_codelet_info(cand, &cl, &cn, cr, &cnr, &cmaxt, &cminb) == 0 && 8 * cn <= cmaxt) id = cand;
+        }
         if (id >= 0) {
             TwiddleBuilder trial = tb;
             InnerPlan ip;
@@ -514,7 +519,10 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
                 int tfc = 1;
                 while (tfc * 2 * cn <= cmaxt && tfc < 8) tfc *= 2;
                 const int64_t twb = (tw_cnt * 8 + 127) & ~int64_t(127);
-                while (tfc > 1 && twb + (int64_t)tfc * wsize * 8 > 72 * 1024) tfc /= 2;
+                // up to 72 KB per CTA (several CTAs per SM) when the launch bound
+                // allows more than one CTA per SM; a single-CTA bound takes all
+                const int64_t cap = cminb > 1 ? 72 * 1024 : kMaxSmemBytes;
+                while (tfc > 1 && twb + (int64_t)tfc * wsize * 8 > cap) tfc /= 2;
                 const int64_t smem = twb + (int64_t)tfc * wsize * 8;
                 // tiles narrower than 8 columns (64-byte row segments) lose more to
                 // sector granularity than the in-place passes gain (measured on
