@@ -454,3 +454,62 @@ def test_twiddles_are_correctly_rounded_fp64_values():
     assert tw.size > 0
     mag = np.abs(tw.astype(np.complex128))
     assert np.abs(mag - 1).max() < 2e-7
+
+
+@pytest.mark.parametrize("kind,n,b", [("c2c", 4096, 64), ("c2c", 4096, 2048), ("c2c", 65536, 3), ("r2c", 3000, 37),
+                                      ("c2r", 3000, 37), ("r2c", 32768, 5), ("c2r", 1024, 9), ("2d", 2048, 1)])
+def test_device_execs_replay_from_a_cuda_graph(kind, n, b):
+    # exec with device pointers only enqueues precomputed launches on the
+    # plan's stream, so it can be captured: one graph of two execs on two
+    # input sets, replayed after the inputs change, matches the FP64 oracle
+    # (cluster, codelet, column-tile and real-data kernels)
+    dev = _dev()
+    s = torch.cuda.Stream(dev)
+    rng = np.random.default_rng(n + b)
+    if kind == "2d":
+        shape_in = shape_out = (b, n, n)
+        plan = A.Plan.plan2d(b, n, n, A.C2C)
+    else:
+        plan = A.Plan.plan1d(n, {"c2c": A.C2C, "r2c": A.R2C, "c2r": A.C2R}[kind], b)
+        shape_in = (b, n) if kind != "c2r" else (b, n // 2 + 1)
+        shape_out = (b, n) if kind != "r2c" else (b, n // 2 + 1)
+    real_in, real_out = kind == "r2c", kind == "c2r"
+    xs = [torch.empty(shape_in, dtype=torch.float32 if real_in else torch.complex64, device=dev) for _ in range(2)]
+    ys = [torch.empty(shape_out, dtype=torch.float32 if real_out else torch.complex64, device=dev) for _ in range(2)]
+
+    def run(i):
+        if kind == "r2c":
+            plan.exec_r2c(xs[i], ys[i])
+        elif kind == "c2r":
+            plan.exec_c2r(xs[i], ys[i])
+        else:
+            plan.exec_c2c(xs[i], ys[i], A.FORWARD)
+
+    with plan:
+        plan.set_stream(s)
+        for x in xs:
+            x.copy_(torch.from_numpy(rng.standard_normal(shape_in).astype(np.float32)) if real_in else
+                    torch.from_numpy((rng.standard_normal(shape_in) + 1j * rng.standard_normal(shape_in))
+                                     .astype(np.complex64)))
+        torch.cuda.synchronize()
+        run(0)  # first exec outside the capture (lazy per-device set-up)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            run(0)
+            run(1)
+        for i, x in enumerate(xs):  # new inputs after the capture
+            x.mul_(-0.5 - i)
+        g.replay()
+        torch.cuda.synchronize()
+        for i in range(2):
+            x = xs[i].cpu().numpy()
+            if kind == "r2c":
+                exact = O.r2c(x)
+            elif kind == "c2r":
+                exact = O.c2r(x, n)
+            elif kind == "2d":
+                exact = np.fft.fft2(x.astype(np.complex128))
+            else:
+                exact = O.c2c(x, -1)
+            _fp64_ok(ys[i].cpu().numpy(), exact, what=f"{kind} {n} graph replay {i}")
