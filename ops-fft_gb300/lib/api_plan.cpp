@@ -165,7 +165,7 @@ void plan_impl_free(PlanImpl* p)
         cudaStreamDestroy(p->s_in);
         cudaStreamDestroy(p->s_out);
         cudaEventDestroy(p->ev_start);
-        for (int c = 0; c < 8; ++c) {
+        for (int c = 0; c < PlanImpl::kMaxHostChunks; ++c) {
             cudaEventDestroy(p->ev_in[c]);
             cudaEventDestroy(p->ev_k[c]);
         }

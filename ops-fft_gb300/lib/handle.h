@@ -43,8 +43,9 @@ struct PlanImpl {
     bool pipe_ready = false;
     cudaStream_t s_in = nullptr, s_out = nullptr;
     cudaEvent_t ev_start = nullptr;
-    cudaEvent_t ev_in[8] = {};
-    cudaEvent_t ev_k[8] = {};
+    static constexpr int kMaxHostChunks = 32;
+    cudaEvent_t ev_in[kMaxHostChunks] = {};
+    cudaEvent_t ev_k[kMaxHostChunks] = {};
 };
 
 void plan_impl_free(PlanImpl* p);
