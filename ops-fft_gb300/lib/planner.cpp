@@ -495,7 +495,18 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     // that codelet (one transform group per column, in-place passes)
     if (Ns == 1 && !staged_out && codelets_enabled()) {
         // the first codelet of this length whose launch bound holds 8 columns
+        // (OPS_FFT_COLTILE_VARIANT=k: the k-th codelet of the length, tiles of
+        // at least 4 columns; tuning experiments)
         int id = -1, cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
+        const char* env_cv = std::getenv("OPS_FFT_COLTILE_VARIANT");
+        int min_tf = 8;
+        if (env_cv) {
+            const int cand = gfft_codelet_find(Lq, std::atoi(env_cv));
+            if (cand >= 0 && gfft_codelet_info(cand, &cl, &cn, cr, &cnr, &cmaxt, &cminb) == 0 && 4 * cn <= cmaxt) {
+                id = cand;
+                min_tf = 4;
+            }
+        }
         for (int k = 0; id < 0; ++k) {
             const int cand = gfft_codelet_find(Lq, k);
             if (cand < 0) break;
@@ -528,7 +539,7 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
                 // sector granularity than the in-place passes gain (measured on
                 // 2048-point columns: 2 columns per tile were 1.7x slower than the
                 // column kernel's 4)
-                if (tfc >= 8 && smem <= kMaxSmemBytes && tw_cnt * 8 <= 64 * 1024) {
+                if (tfc >= min_tf && smem <= kMaxSmemBytes && tw_cnt * 8 <= 64 * 1024) {
                     tb = trial;
                     a.ip = ip;
                     a.codelet = id;
