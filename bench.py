@@ -54,6 +54,24 @@ NCU_TRAFFIC = {
 }
 
 
+def max_over_ranks(x, dist, device):
+    """x maximised over all ranks of the process group (x itself without one).
+    Every rank runs a full replica of the workload on its own GPU, so the
+    whole job lasts as long as the slowest rank."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gbs(alg_bytes_per_step, world, steps, seconds):
+    """Algorithmic bytes of all ranks' steps per second of the slowest rank."""
+    return alg_bytes_per_step * world * steps / seconds / 1e9
+
+
 def _peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -844,12 +862,9 @@ def main():
     time.sleep(0.3)
     ms, dom_ms, per_item = timed(nk)
     clk = clocks.stop()
-    if dist:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = max_over_ranks(ms, dist, dev)
     ms_per_step = ms / nk
-    value = wl.alg_bytes_per_step * world * nk / (ms / 1e3) / 1e9
+    value = whole_job_gbs(wl.alg_bytes_per_step, world, nk, ms / 1e3)
 
     peak, peak_kind = _peaks()
     achieved = wl.dominant[1] / (dom_ms / 1e3) / 1e9
@@ -873,11 +888,8 @@ def main():
             wl.step_host()
         torch.cuda.synchronize()
         te = time.perf_counter() - ts
-        if dist:
-            tt = torch.tensor([te], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        e2e = {"value": round(wl.alg_bytes_per_step * world * ke / te / 1e9, 2), "unit": "GB/s",
+        te = max_over_ranks(te, dist, dev)
+        e2e = {"value": round(whole_job_gbs(wl.alg_bytes_per_step, world, ke, te), 2), "unit": "GB/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "path": "aclfftExec* with pinned host buffers (library stages and synchronises)"}
 
