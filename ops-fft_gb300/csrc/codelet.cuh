@@ -393,22 +393,38 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
             //   X[k] = E + W^k O, X[L-k] = conj(E - W^k O),
             //   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0 (zero imaginary parts)
+            // every pair of the thread is read (and its twiddle) before any
+            // is stored, so the shared loads of all its pairs are in flight
+            // together
             const float sc = A.scale;
             const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
-            for (int k = tid; k <= (L >> 1); k += S::NTHR) {
+            constexpr int NPO = (L / 2 + 1 + S::NTHR - 1) / S::NTHR;  // pairs per thread
+            float2 za[NPO], zb[NPO], wk[NPO];
+            sfor<NPO>([&](auto qq) {
+                constexpr int q = decltype(qq)::value;
+                const int k = tid + q * S::NTHR;
+                if (k <= (L >> 1)) {
+                    za[q] = W[cpad<S>(k)];
+                    zb[q] = W[cpad<S>(L - k)];  // k = 0: entry L, unused
+                    wk[q] = post[k];
+                }
+            });
+            sfor<NPO>([&](auto qq) {
+                constexpr int q = decltype(qq)::value;
+                const int k = tid + q * S::NTHR;
                 if (k == 0) {
-                    const float2 z0 = W[0];
+                    const float2 z0 = za[q];
                     c.out2[0] = make_float2((z0.x + z0.y) * sc, 0.f);
                     c.out2[L] = make_float2((z0.x - z0.y) * sc, 0.f);
-                } else {
-                    const float2 zk = W[cpad<S>(k)], zc = cconj(W[cpad<S>(L - k)]);
+                } else if (k <= (L >> 1)) {
+                    const float2 zk = za[q], zc = cconj(zb[q]);
                     const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
                     const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
-                    const float2 wo = cmul(post[k], o);
+                    const float2 wo = cmul(wk[q], o);
                     c.out2[k] = cscale(cadd(e, wo), s2);
                     if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
                 }
-            }
+            });
             group_sync<S>(bar_id);
         }
         // the slot is free: refill it with the transform NST iterations ahead
