@@ -3,7 +3,9 @@
 // with MINB CTAs per SM (register cap 65536 / (MAXT * MINB)).  The first
 // entry of a length is the spill-free build with the higher register cap,
 // measured faster than the 80-register builds kept as variants (up to 1.2x
-// for 1024-4096 points, whose 80-register builds spill); the planner
+// for 1024-4096 points, whose 80-register builds spill), and for 128/256
+// points the radix order that keeps all 32 lanes of the transform's warp
+// busy (8*8*4: 1.17x, 4*4*8: 1.11x over 16*16 and 8*16); the planner
 // picks the first entry whose length matches exactly, or the k-th one with
 // OPS_FFT_CODELET_VARIANT=k (entries after the first for a length are
 // variants: other register caps or radix orders; a column pass takes the
@@ -17,8 +19,8 @@
     X(2, 256, 2, 4096, 256, 16, 16, 16)        \
     X(3, 256, 2, 2048, 128, 16, 16, 8)         \
     X(4, 256, 2, 1024, 64, 16, 16, 4)          \
-    X(5, 384, 2, 256, 32, 16, 16)              \
-    X(6, 384, 2, 128, 32, 8, 16)               \
+    X(5, 256, 2, 256, 32, 8, 8, 4)             \
+    X(6, 256, 2, 128, 32, 4, 4, 8)             \
     X(7, 512, 1, 8192, 512, 16, 16, 16, 2)     \
     X(8, 160, 6, 1500, 160, 15, 10, 10)        \
     X(9, 128, 8, 512, 64, 8, 8, 8)             \
@@ -27,5 +29,7 @@
     X(12, 384, 2, 2048, 128, 16, 16, 8)        \
     X(13, 384, 2, 1024, 64, 16, 16, 4)         \
     X(14, 384, 2, 1500, 160, 15, 10, 10)       \
-    X(15, 384, 2, 512, 64, 8, 8, 8)
-#define GFFT_NUM_CODELETS 16
+    X(15, 384, 2, 512, 64, 8, 8, 8)            \
+    X(16, 384, 2, 256, 32, 16, 16)             \
+    X(17, 384, 2, 128, 32, 8, 16)
+#define GFFT_NUM_CODELETS 18
