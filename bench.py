@@ -154,6 +154,7 @@ class Cfg2:
         self.sets = []
         self.plans = {}
         self.stream = stream
+        self.dev = dev
         self.side = torch.cuda.Stream(dev)
         self.streams = {3000: stream, 1024: self.side}
         for n in self.sizes:
@@ -221,15 +222,31 @@ class Cfg2:
         return h2d, d2h
 
     def step_host(self):
-        for n in self.sizes:
-            h = self.host[n]
-            pr, pc = self.plans[n]
-            # host buffers: each exec copies in, runs and synchronises its
-            # plan's stream (the reference's calling convention), one after
-            # the other
-            pr.exec_r2c(h["x"], h["X"])
-            pc.exec_c2r(h["X"], h["y"])
-            pr.exec_r2c_adjoint(h["G"], h["gx"])
+        # host buffers: each exec copies in, runs and synchronises its plan's
+        # stream (the reference's calling convention).  The two lengths are
+        # independent plans, so the N=1024 chain runs on a second host thread
+        # (distinct plans may be used concurrently; ctypes releases the GIL)
+        import threading
+
+        errors = []
+
+        def chain(n):
+            try:
+                self.torch.cuda.set_device(self.dev)
+                h = self.host[n]
+                pr, pc = self.plans[n]
+                pr.exec_r2c(h["x"], h["X"])
+                pc.exec_c2r(h["X"], h["y"])
+                pr.exec_r2c_adjoint(h["G"], h["gx"])
+            except Exception as e:  # noqa: BLE001 - re-raised on the calling thread
+                errors.append(e)
+
+        side = threading.Thread(target=chain, args=(1024,))
+        side.start()
+        chain(3000)
+        side.join()
+        if errors:
+            raise errors[0]
 
     # CPU baseline: FP32 port of the reference path on a sample of rows
     def cpu_sample(self, O, rows, nthreads):
