@@ -897,7 +897,7 @@ def main():
         for _ in range(2):
             wl.step_host()
         torch.cuda.synchronize()
-        ke = 3 if isinstance(wl, LongWorkload) else max(3, min(nk, 10))
+        ke = 3 if isinstance(wl, LongWorkload) else max(3, min(nk, 30))
         if dist:
             dist.barrier()
         ts = time.perf_counter()
