@@ -371,3 +371,23 @@ def test_tc_index_maps_match_numpy_emulation():
             tc_pass(ws, L2, b * L1, L1, n, L2, 1, n, 1, L1, 1, out)
         e = O.errors(out, O.c2c(x.reshape(b, n), -1))
         assert e["rel_l2"] < 1e-13, (n, b, e)
+
+
+@pytest.mark.parametrize("variant", ["0", "1", "2"])
+def test_codelet_variants_and_cluster_choices_stay_in_bounds(variant, monkeypatch):
+    """Every specialised build of a length (OPS_FFT_CODELET_VARIANT) and both
+    kernel families of the short cluster lengths (batches below and above
+    OPS_FFT_CLUSTER_MAXBATCH) pass the host replay of their launches."""
+    monkeypatch.setenv("OPS_FFT_CODELET_VARIANT", variant)
+    for n in (256, 512, 1024, 2048, 3000, 4096, 8192):
+        for typ in (A.C2C, A.R2C, A.C2R):
+            for b in (7, 1500):
+                with A.Plan.plan1d(n, typ, b) as p:
+                    assert p.check() == "ok"
+    for b, want in ((1024, True), (1025, False)):
+        with A.Plan.plan1d(4096, A.C2C, b) as p:
+            assert (p.info().cluster_ctas > 0) == want
+            assert p.check() == "ok"
+    monkeypatch.setenv("OPS_FFT_COLTILE_VARIANT", variant)
+    with A.Plan.plan2d(3, 2048, 2048, A.C2C) as p:
+        assert p.check() == "ok"
