@@ -19,6 +19,8 @@
 #include <cstring>
 #include <new>
 
+#include <cstdlib>
+
 #include "handle.h"
 
 using gfft::Kind;
@@ -241,7 +243,10 @@ aclfftResult plan_device_setup(PlanImpl* p)
                                cudaGetErrorString((cudaError_t)(n < 0 ? -n : (int)cudaErrorInvalidConfiguration)));
                 return ACLFFT_SETUP_FAILED;
             }
-            s.cl.clusters = n;
+            // OPS_FFT_CLUSTER_COUNT=<k> launches at most k clusters (tuning)
+            const char* env_cc = std::getenv("OPS_FFT_CLUSTER_COUNT");
+            const int cap = env_cc ? std::atoi(env_cc) : 0;
+            s.cl.clusters = (cap > 0 && cap < n) ? cap : n;
         }
     }
     p->device = dev;
