@@ -152,8 +152,10 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
     // shorten the pipeline's fill and drain but cost more per chunk; measured
     // on the R2C/C2R N=3000/1024 batch-4096 round trip with pinned buffers:
     // 4 chunks 230 GB/s, 8 224, 16 209, 32 178
-    const char* env_ch = std::getenv("OPS_FFT_HOST_CHUNKS");
-    const int kChunks = env_ch ? std::max(2, std::min(PlanImpl::kMaxHostChunks, std::atoi(env_ch))) : 4;
+    static const int kChunks = [] {
+        const char* v = std::getenv("OPS_FFT_HOST_CHUNKS");
+        return v ? std::max(2, std::min(PlanImpl::kMaxHostChunks, std::atoi(v))) : 4;
+    }();
     if (ntf < 2 * kChunks || in_bytes + out_bytes < (size_t)(8u << 20)) return -1;
     if (in_bytes % (size_t)ntf || out_bytes % (size_t)ntf) return -1;
     const size_t rin = in_bytes / (size_t)ntf, rout = out_bytes / (size_t)ntf;
