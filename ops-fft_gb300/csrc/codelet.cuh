@@ -106,9 +106,10 @@ __device__ __forceinline__ void group_sync(int id)
 
 // One in-place pass P of codelet S on the transform held in W (shared) or,
 // for P == 0 with from_slot, read from the slot copy through c.gload.
-template <class S, int P>
+template <class S, int P, bool FC2R = false>
 __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2 (&v)[S::E], const float2* tw,
-                                             int tw_off, bool from_slot, bool last_global, int bar_id)
+                                             int tw_off, bool from_slot, bool last_global, int bar_id,
+                                             const float2* post = nullptr)
 {
     constexpr int R = S::R[P];
     constexpr int NS = S::ns(P);
@@ -131,7 +132,31 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
                 }
             });
         };
-        if (c.mode == IO_R2C_ODD) {
+        if constexpr (FC2R) {
+            // even C2R with the Hermitian pre-process fused into this first
+            // pass: Z'[i] from the raw bins X[i] and X[L-i] of the slot
+            // (X[L] for i = 0), stored conjugated for the forward transform:
+            //   k = min(i, L-i), E = X[k] + conj X[L-k],
+            //   O = (X[k] - conj X[L-k]) * conj W_N^k,
+            //   Z'[k] = conj(E + iO), Z'[L-k] = conj(conj(E) + i conj(O)),
+            //   Z'[0] = (x0 + xL, -(x0 - xL)) (imaginary parts of DC and Nyquist ignored)
+            constexpr int L = S::L;
+            const bool half = c.weight == WEIGHT_LOAD_HALF;
+            load_all([&](int i) {
+                const float2 xi = c.st2[i], xm = c.st2[L - i];
+                if (i == 0) return make_float2(xi.x + xm.x, -(xi.x - xm.x));
+                const bool lo = i <= (L >> 1);
+                float2 a = lo ? xi : xm, b = lo ? xm : xi;  // a = X[k], b = X[L-k]
+                if (half) {
+                    a = cscale(a, 0.5f);
+                    b = cscale(b, 0.5f);
+                }
+                const float2 bc = cconj(b);
+                const float2 e = cadd(a, bc);
+                const float2 o = cmulc(csub(a, bc), post[lo ? i : L - i]);
+                return lo ? cconj(make_float2(e.x - o.y, e.y + o.x)) : cconj(make_float2(e.x + o.y, -e.y + o.x));
+            });
+        } else if (c.mode == IO_R2C_ODD) {
             load_all([&](int i) { return make_float2(c.st1[i], 0.f); });
         } else if (c.mode == IO_C2R_ODD) {
             load_all([&](int i) { return c.gload(i); });
@@ -231,7 +256,9 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
 // superset only touches bytes of the neighbouring rows of the same buffer;
 // when it would reach outside the buffer (first/last row with unaligned
 // ends) the group copies the row with ordinary loads instead.
-template <class S>
+// FC2R: the even-C2R instance (pre-process fused into the first pass, see
+// codelet_pass); the plain instance serves every mode.
+template <class S, bool FC2R = false>
 __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_constant__ RowArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
@@ -344,7 +371,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         c.out1 = reinterpret_cast<float*>(A.out) + t * A.out_dist;
 
         bool from_slot = true;
-        if (A.io_mode == IO_C2R_EVEN) {
+        if (!FC2R && A.io_mode == IO_C2R_EVEN) {
             // pre-process pairs (k, L-k) in place:
             //   Z'[k] = E + i*O,  E = X[k] + conj(X[L-k]),
             //   O = (X[k] - conj(X[L-k])) * conj(W_N^k), stored conjugated.
@@ -383,7 +410,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             group_sync<S>(bar_id);
             from_slot = false;
         }
-        codelet_pass<S, 0>(c, W, v, tw, A.ip.pass[0].tw_off, from_slot, last_global, bar_id);
+        codelet_pass<S, 0, FC2R>(c, W, v, tw, A.ip.pass[0].tw_off, from_slot, last_global, bar_id, post);
         sfor<S::NP - 1>([&](auto pp) {
             constexpr int P = decltype(pp)::value + 1;
             codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off, false, last_global, bar_id);

@@ -18,13 +18,27 @@ struct CodeletSpec;
 GFFT_CODELETS(GFFT_SPEC_OF)
 #undef GFFT_SPEC_OF
 
+// Lengths whose even-C2R launches use the instance with the pre-process fused
+// into the first pass (a second kernel per length, so the plain instance's
+// register allocation is unchanged).  Measured: C2R N=1024 12.7 -> 11.5 us
+// (batch 4096); no gain for the 1500-point codelet (N=3000), which keeps
+// the separate pre-process.
+template <class S>
+constexpr bool fuse_c2r()
+{
+    return S::L == 512 || S::L == 1024 || S::L == 2048;
+}
+
 }  // namespace gfft
 
 #define GFFT_CODELET_TU(ID)                                                              \
     namespace gfft {                                                                     \
     int launch_codelet_##ID(const RowArgs* a, cudaStream_t st)                           \
     {                                                                                    \
-        return launch_codelet_t<CodeletSpec<ID>::type>(a, st);                           \
+        using S_ = CodeletSpec<ID>::type;                                                \
+        if constexpr (fuse_c2r<S_>())                                                    \
+            if (a->io_mode == IO_C2R_EVEN) return launch_codelet_t<S_, true>(a, st);    \
+        return launch_codelet_t<S_>(a, st);                                              \
     }                                                                                    \
     int launch_coltile_##ID(const ColArgs* a, cudaStream_t st)                           \
     {                                                                                    \

@@ -78,7 +78,7 @@ int launch_col_t(const ColArgs* a, cudaStream_t st)
     return (int)cudaGetLastError();
 }
 
-template <class S>
+template <class S, bool FC2R = false>
 int launch_codelet_t(const RowArgs* a, cudaStream_t st)
 {
     static unsigned long long attr_mask = 0;
@@ -88,11 +88,11 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
         return (int)cudaErrorInvalidValue;
     if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
         return (int)cudaErrorInvalidValue;
-    cudaError_t e = ensure_smem_attr(codelet_kernel<S>, attr_mask, (size_t)a->smem_bytes);
+    cudaError_t e = ensure_smem_attr(codelet_kernel<S, FC2R>, attr_mask, (size_t)a->smem_bytes);
     if (e != cudaSuccess) return (int)e;
     if (threads != last_threads || a->smem_bytes != last_smem) {
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, codelet_kernel<S>, threads, (size_t)a->smem_bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, codelet_kernel<S, FC2R>, threads, (size_t)a->smem_bytes);
         if (e != cudaSuccess) return (int)e;
         last_threads = threads;
         last_smem = a->smem_bytes;
@@ -104,7 +104,7 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
     if (a->grid > 0) grid = a->grid;
     if (grid < 1) grid = 1;
     if (grid > ctas_needed) grid = ctas_needed;
-    codelet_kernel<S><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
+    codelet_kernel<S, FC2R><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
     return (int)cudaGetLastError();
 }
 
