@@ -14,6 +14,14 @@
 extern "C" {
 #endif
 
+/* Library version reported by aclfftGetVersion (MAJOR*10000 + MINOR*100 +
+ * PATCH) and aclfftGetProperty. */
+#define ACLFFT_GB300_VERSION_MAJOR 1
+#define ACLFFT_GB300_VERSION_MINOR 1
+#define ACLFFT_GB300_VERSION_PATCH 0
+#define ACLFFT_GB300_VERSION \
+    (ACLFFT_GB300_VERSION_MAJOR * 10000 + ACLFFT_GB300_VERSION_MINOR * 100 + ACLFFT_GB300_VERSION_PATCH)
+
 /* Normalisation.  The reference fixes normMode = 0 (lib/fft_handle_impl.h:36):
  * neither direction is scaled.  The other modes scale by the total number
  * of points n of one transform (nx for 1D, nx*ny for 2D). */
@@ -90,6 +98,16 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
 ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host, long long maxEntries,
                                           long long* entries);
 
+/* Layout of the twiddle blob returned by aclfftGetTwiddles (for tests):
+ * per segment five values {offset, count, M, param, kind}; entry i of the
+ * segment (at blob index offset + i) is exp(-2 pi i m / M) evaluated in
+ * FP64 and rounded to FP32, with m = (i / param) * (i % param) mod M for a
+ * pass table (kind 2, layout [r][k] with param = k's extent) and
+ * m = i * param mod M for a linear table (kind 1); kind 3 segments hold
+ * tensor-core DFT-matrix operand images.  Writes at most maxSegs segments;
+ * *nsegs receives the total. */
+ACLFFT_API aclfftResult aclfftDebugGetTwiddleSegments(aclfftHandle plan, long long* segs, int maxSegs, int* nsegs);
+
 /* Allocation-free long C2C (no counterpart in the reference).  For callers
  * that cannot allocate device memory - code running while another component
  * owns the device memory pool, or that must avoid cudaMalloc/cudaFree and
@@ -150,8 +168,19 @@ ACLFFT_API aclfftResult aclfftRaggedAutotune(aclfftRaggedPlan plan);
 ACLFFT_API aclfftResult aclfftRaggedExec(aclfftRaggedPlan plan, void* idata, void* odata, int direction);
 ACLFFT_API aclfftResult aclfftRaggedGetInfo(aclfftRaggedPlan plan, aclfftRaggedInfo* info);
 /* Device error flags of the plan's launches (bit 2: a dependency wait ran
- * out of time); synchronises with the device. */
+ * out of time, the items behind it were skipped and the output is
+ * incomplete).  Synchronises the plan's stream, stores the flags in *flags,
+ * clears them and returns ACLFFT_EXEC_FAILED when any was set. */
 ACLFFT_API aclfftResult aclfftRaggedGetError(aclfftRaggedPlan plan, int* flags);
+/* Upper bound, in SM clock cycles, of each dependency wait inside the
+ * ragged kernel (default 2^31, about a second; must be > 0).  Takes effect
+ * at the next exec. */
+ACLFFT_API aclfftResult aclfftRaggedSetWaitLimit(aclfftRaggedPlan plan, long long cycles);
+/* Test hook: every dependency wait of the next execs waits for `extra` more
+ * completed items than exist (0 restores normal operation), so a wait runs
+ * out of time by construction and the failure path can be exercised without
+ * faulting the GPU. */
+ACLFFT_API aclfftResult aclfftRaggedDebugHoldDependencies(aclfftRaggedPlan plan, int extra);
 ACLFFT_API aclfftResult aclfftRaggedDestroy(aclfftRaggedPlan plan);
 /* Host replay of every work item's index ranges (0 = all in bounds). */
 ACLFFT_API int aclfftRaggedDebugCheck(aclfftRaggedPlan plan, char* msg, int msglen);
@@ -160,6 +189,32 @@ ACLFFT_API int aclfftRaggedDebugCheck(aclfftRaggedPlan plan, char* msg, int msgl
  * the buffer sizes of each call variant (no kernel runs).  Returns 0 when
  * all launches stay in bounds; msg receives a description. */
 ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int msglen);
+
+/* Device-side failure reporting (no counterpart in the reference, whose
+ * execs are synchronous and map a failed kernel to ACLFFT_EXEC_FAILED,
+ * src/fft1_d/arch32/fft1_d_exec_api.cpp:148-152).  Every wait inside the
+ * kernels is bounded; a wait that runs out sets a bit in the plan's device
+ * error word and the kernel returns early, leaving the output incomplete:
+ *   bit 0  row kernel: an input copy did not arrive
+ *   bit 1  tensor-core stage: an MMA did not complete
+ *   bit 3  cluster kernel: a distributed-shared-memory exchange did not arrive
+ * Execs on host buffers read the word before returning (they synchronise
+ * anyway) and return ACLFFT_EXEC_FAILED when a bit is set.  Execs on device
+ * buffers are asynchronous: aclfftGetExecError synchronises the plan's
+ * stream, stores the word in *flags, clears it and returns
+ * ACLFFT_EXEC_FAILED when it was non-zero (ACLFFT_SUCCESS otherwise).  The
+ * word accumulates over execs until it is read. */
+ACLFFT_API aclfftResult aclfftGetExecError(aclfftHandle plan, int* flags);
+/* Test hook: overwrites the plan's device error word with `flags` (on the
+ * plan's stream, synchronously), as a kernel whose wait ran out would. */
+ACLFFT_API aclfftResult aclfftDebugSetExecError(aclfftHandle plan, int flags);
+
+/* Test hook for allocation failures: after `after` more successful device
+ * allocations (after >= 0) every device allocation the library makes fails
+ * as if cudaMalloc had run out of memory, so that ACLFFT_ALLOC_FAILED paths
+ * can be exercised; a negative value switches the hook off (the default).
+ * Process-wide. */
+ACLFFT_API aclfftResult aclfftDebugFailAllocations(int after);
 
 /* Human-readable reason of the last failure on this thread ("" if none). */
 ACLFFT_API const char* aclfftGetLastErrorDetail(void);

@@ -154,6 +154,12 @@ _SIGNATURES = {
     "aclfftRaggedGetError": [_H, ctypes.POINTER(_I)],
     "aclfftRaggedDestroy": [_H],
     "aclfftRaggedDebugCheck": [_H, ctypes.c_char_p, _I],
+    "aclfftRaggedSetWaitLimit": [_H, ctypes.c_longlong],
+    "aclfftRaggedDebugHoldDependencies": [_H, _I],
+    "aclfftGetExecError": [_H, ctypes.POINTER(_I)],
+    "aclfftDebugSetExecError": [_H, _I],
+    "aclfftDebugFailAllocations": [_I],
+    "aclfftDebugGetTwiddleSegments": [_H, _VP, _I, ctypes.POINTER(_I)],
 }
 
 
@@ -256,6 +262,26 @@ class Plan:
     def exec_c2r_adjoint(self, g_out, g_in) -> None:
         _check(lib().aclfftExecC2RAdjoint(self.handle, ptr(g_out), ptr(g_in)), "aclfftExecC2RAdjoint")
 
+    def exec_error(self) -> int:
+        """Synchronises the plan's stream and returns (and clears) the device
+        error flags of its execs (0: every bounded wait completed)."""
+        f = _I()
+        rc = lib().aclfftGetExecError(self.handle, ctypes.byref(f))
+        if rc not in (SUCCESS, EXEC_FAILED):
+            _check(rc, "aclfftGetExecError")
+        return f.value
+
+    def work_size(self) -> int:
+        sz = ctypes.c_size_t()
+        _check(lib().aclfftGetSize(self.handle, ctypes.byref(sz)), "aclfftGetSize")
+        return sz.value
+
+    def set_auto_allocation(self, on: bool) -> None:
+        _check(lib().aclfftSetAutoAllocation(self.handle, int(bool(on))), "aclfftSetAutoAllocation")
+
+    def set_work_area(self, area) -> None:
+        _check(lib().aclfftSetWorkArea(self.handle, ptr(area) or None), "aclfftSetWorkArea")
+
     def info(self) -> PlanInfo:
         inf = PlanInfo()
         _check(lib().aclfftGetPlanInfo(self.handle, ctypes.byref(inf)), "aclfftGetPlanInfo")
@@ -269,6 +295,17 @@ class Plan:
         out = np.zeros(n.value, dtype=np.complex64)
         _check(lib().aclfftGetTwiddles(self.handle, out.ctypes.data, n.value, ctypes.byref(n)), "aclfftGetTwiddles")
         return out
+
+    def twiddle_segments(self):
+        """(offset, count, M, param, kind) of every segment of the twiddle blob."""
+        import numpy as np
+
+        n = _I()
+        _check(lib().aclfftDebugGetTwiddleSegments(self.handle, None, 0, ctypes.byref(n)), "aclfftDebugGetTwiddleSegments")
+        out = np.zeros((max(n.value, 1), 5), dtype=np.int64)
+        _check(lib().aclfftDebugGetTwiddleSegments(self.handle, out.ctypes.data, n.value, ctypes.byref(n)),
+               "aclfftDebugGetTwiddleSegments")
+        return [tuple(int(v) for v in row) for row in out[: n.value]]
 
     def check(self) -> str:
         """Host-side bounds check of every launch of the plan ('ok' or why)."""
@@ -336,9 +373,20 @@ class RaggedPlan:
         return inf
 
     def error_flags(self) -> int:
+        """Synchronises the plan's stream and returns (and clears) the device
+        error flags (bit 2: a dependency wait ran out of time)."""
         f = _I()
-        _check(lib().aclfftRaggedGetError(self.handle, ctypes.byref(f)), "aclfftRaggedGetError")
+        rc = lib().aclfftRaggedGetError(self.handle, ctypes.byref(f))
+        if rc not in (SUCCESS, EXEC_FAILED):
+            _check(rc, "aclfftRaggedGetError")
         return f.value
+
+    def set_wait_limit(self, cycles: int) -> None:
+        _check(lib().aclfftRaggedSetWaitLimit(self.handle, int(cycles)), "aclfftRaggedSetWaitLimit")
+
+    def debug_hold_dependencies(self, extra: int) -> None:
+        _check(lib().aclfftRaggedDebugHoldDependencies(self.handle, int(extra)),
+               "aclfftRaggedDebugHoldDependencies")
 
     def check(self) -> str:
         buf = ctypes.create_string_buffer(256)

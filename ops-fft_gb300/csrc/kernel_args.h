@@ -234,7 +234,7 @@ struct RagArgs {
     int32_t nitems;
     int32_t smem_bytes;
     int32_t ctas;   // persistent CTAs to launch (gfft_ragged_ctas * SM count)
-    int32_t pad_;
+    int32_t need_bias;  // added to every dependency count (test hook; 0 normally)
     int* queue;     // queue[0]: next item; queue[1 + x]: completed items of transform x
     int* err;
     const void* tw;
@@ -243,6 +243,7 @@ struct RagArgs {
     void* ws;  // float2 workspace
     int32_t inverse;  // C2C transforms run backward (R2C transforms are always forward)
     float scale_c2c;  // applied to C2C outputs
+    long long wait_cycles;  // bound of each dependency wait (SM clock cycles)
 };
 
 // Long C2C transforms on a thread-block cluster (csrc/cluster_fft.cu).  The

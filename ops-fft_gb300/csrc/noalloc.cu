@@ -22,8 +22,9 @@
 //   * the first call on a device resolves the arrays' device addresses with
 //     cudaGetSymbolAddress (once per device), so that first call should
 //     happen before any stream capture;
-//   * idata and odata must be device (or managed) pointers; idata == odata is
-//     allowed because the intermediate never touches the caller's buffers.
+//   * idata and odata must be device pointers of the current device (or
+//     managed pointers); idata == odata is allowed because the intermediate
+//     never touches the caller's buffers.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -76,14 +77,18 @@ cudaError_t device_addrs(int dev, DeviceAddrs& out)
     return cudaSuccess;
 }
 
-bool is_device_pointer(const void* p)
+// Device memory of the current device `dev`, or managed memory.  Device
+// memory of another GPU is refused: the kernels would dereference it as a
+// peer address, which faults when peer access is not enabled.
+bool is_local_device_pointer(const void* p, int dev)
 {
     cudaPointerAttributes at;
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeDevice && at.device == dev;
 }
 
 aclfftResult fail(aclfftResult code, const std::string& why)
@@ -104,8 +109,14 @@ extern "C" ACLFFT_API aclfftResult aclfftExecC2CNoAlloc(const aclfftComplex* ida
         return fail(ACLFFT_INVALID_VALUE, "direction must be ACLFFT_FORWARD or ACLFFT_BACKWARD");
     if ((long long)nx * (long long)batch > kScratchElems)
         return fail(ACLFFT_INVALID_SIZE, "nx * batch exceeds the 2^21-element scratch of the allocation-free entry");
-    if (!is_device_pointer(idata) || !is_device_pointer(odata))
-        return fail(ACLFFT_INVALID_VALUE, "the allocation-free entry takes device pointers only");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return fail(ACLFFT_EXEC_FAILED, "no current CUDA device");
+    }
+    if (!is_local_device_pointer(idata, dev) || !is_local_device_pointer(odata, dev))
+        return fail(ACLFFT_INVALID_VALUE,
+                    "the allocation-free entry takes device pointers of the current device only");
 
     gfft::TwiddleBuilder tb;
     std::vector<gfft::Step> steps;
@@ -113,11 +124,6 @@ extern "C" ACLFFT_API aclfftResult aclfftExecC2CNoAlloc(const aclfftComplex* ida
         return fail(ACLFFT_NOT_IMPLEMENTED, "nx does not split into two on-chip factors (prime factors <= 47)");
     if (tb.count > kTwiddleElems) return fail(ACLFFT_INVALID_SIZE, "twiddle tables exceed the fixed table size");
 
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        cudaGetLastError();
-        return fail(ACLFFT_EXEC_FAILED, "no current CUDA device");
-    }
     DeviceAddrs a;
     const cudaError_t e = device_addrs(dev, a);
     if (e != cudaSuccess) {

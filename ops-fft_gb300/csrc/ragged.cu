@@ -113,13 +113,14 @@ __device__ __forceinline__ const float2* stage_twiddles(const float2* tw, int64_
     return dst - lo;
 }
 
-__device__ __forceinline__ bool wait_count(int* ctr, int need, int* err)
+__device__ __forceinline__ bool wait_count(int* ctr, int need, int* err, long long budget)
 {
+    if (budget <= 0) budget = 1ll << 31;
     const long long t0 = clock64();
     while (atomicAdd(ctr, 0) < need) {
         if (*reinterpret_cast<volatile int*>(err) & 4) return false;
         __nanosleep(128);
-        if (clock64() - t0 > (1ll << 31)) {
+        if (clock64() - t0 > budget) {
             atomicOr(err, 4);
             return false;
         }
@@ -146,7 +147,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
         const RagClass& C = A.cls[item.cls];
         const int type = C.type;
         if (item.kind == RAG_P2 || item.kind == RAG_POST) {
-            if (threadIdx.x == 0) s_ok = wait_count(A.queue + 1 + item.xform, item.need, A.err) ? 1 : 0;
+            if (threadIdx.x == 0) s_ok = wait_count(A.queue + 1 + item.xform, item.need + A.need_bias, A.err, A.wait_cycles) ? 1 : 0;
             __syncthreads();
             if (!s_ok) continue;
         }

@@ -14,6 +14,7 @@
 // through plan-owned device buffers and the call synchronises the stream
 // before returning, which is the reference's contract for host buffers.
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <thread>
 
@@ -27,14 +28,47 @@ namespace {
 
 thread_local std::string g_last_error;
 
-bool device_accessible(const void* p)
+// Where a caller's buffer lives: host memory (pageable or pinned) is staged
+// through the plan's device buffers; device memory must belong to the device
+// the call runs on (another GPU's memory would be dereferenced as a peer
+// address, which faults without peer access); managed memory is reachable
+// from every device.
+enum class Mem { HOST, DEVICE, FOREIGN };
+
+Mem classify(const void* p, int dev)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return Mem::HOST;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return Mem::DEVICE;
+    if (a.type == cudaMemoryTypeDevice) return a.device == dev ? Mem::DEVICE : Mem::FOREIGN;
+    return Mem::HOST;
+}
+
+// Reads (and clears) the plan's device error word after the work queued on
+// `st`; every bounded wait in the kernels sets a bit there when it gives up
+// (bit 0 row-kernel copy wait, bit 1 tensor-core MMA wait, bit 3 cluster
+// exchange wait).  Synchronises `st`.
+aclfftResult drain_error_word(PlanImpl* impl, cudaStream_t st, int* flags_out)
+{
+    int v = 0;
+    if (cudaMemcpyAsync(&v, impl->err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        gfft::set_last_error("reading the device error word failed");
+        return ACLFFT_EXEC_FAILED;
+    }
+    if (flags_out) *flags_out = v;
+    if (v == 0) return ACLFFT_SUCCESS;
+    if (cudaMemsetAsync(impl->err, 0, sizeof(int), st) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess)
+        cudaGetLastError();
+    char msg[96];
+    std::snprintf(msg, sizeof msg, "a device wait ran out of time (error flags 0x%x); the output is incomplete", v);
+    gfft::set_last_error(msg);
+    GFFT_LOG("exec: %s", msg);
+    return ACLFFT_EXEC_FAILED;
 }
 
 double points(const aclfftHandle_t* h)
@@ -139,6 +173,24 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
     return 0;
 }
 
+// True when a step of `sl` reads or writes a workspace the plan does not
+// have (auto allocation off and no work area set).
+bool missing_workspace(const PlanImpl* impl, const StepList& sl)
+{
+    for (const Step& s : sl.steps) {
+        for (int b : {s.src, s.dst}) {
+            if ((b == 2 && !impl->ws) || (b == 3 && !impl->ws2)) return true;
+        }
+    }
+    return false;
+}
+
+aclfftResult no_workspace()
+{
+    gfft::set_last_error("the plan has no work area: auto allocation is off and aclfftSetWorkArea was not called");
+    return ACLFFT_NO_WORKSPACE;
+}
+
 // Host buffers, one row-kernel step: the batch is cut into chunks whose
 // host-to-device copy, kernel and device-to-host copy run on three streams,
 // so copies in both directions overlap the kernels of neighbouring chunks.
@@ -182,12 +234,23 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
         if (t0 >= t1) break;
         ++used;
         char* din = static_cast<char*>(impl->stage_a) + t0 * rin;
-        char* dout = static_cast<char*>(impl->stage_b) + t0 * rout;
         if (cudaMemcpyAsync(din, static_cast<const char*>(in) + t0 * rin, (t1 - t0) * rin, cudaMemcpyHostToDevice,
                             impl->s_in) != cudaSuccess ||
-            cudaEventRecord(impl->ev_in[c], impl->s_in) != cudaSuccess ||
-            cudaStreamWaitEvent(st, impl->ev_in[c], 0) != cudaSuccess)
+            cudaEventRecord(impl->ev_in[c], impl->s_in) != cudaSuccess)
             return 1;
+    }
+    // When the caller's input and output ranges overlap (an in-place call),
+    // a chunk's output rows can cover input rows of later chunks (R2C rows
+    // grow from n reals to n/2+1 complex values), so no result is copied
+    // back before the whole input has been read.
+    const bool overlap = static_cast<const char*>(in) < static_cast<const char*>(out) + out_bytes &&
+                         static_cast<const char*>(out) < static_cast<const char*>(in) + in_bytes;
+    if (overlap && cudaStreamWaitEvent(impl->s_out, impl->ev_in[used - 1], 0) != cudaSuccess) return 1;
+    for (int c = 0; c < used; ++c) {
+        const int64_t t0 = c * per, t1 = std::min<int64_t>(ntf, t0 + per);
+        char* din = static_cast<char*>(impl->stage_a) + t0 * rin;
+        char* dout = static_cast<char*>(impl->stage_b) + t0 * rout;
+        if (cudaStreamWaitEvent(st, impl->ev_in[c], 0) != cudaSuccess) return 1;
         gfft::RowArgs a = step.row;
         a.tw = tw;
         a.post_tw = step.post_off >= 0 ? tw + step.post_off : nullptr;
@@ -206,7 +269,6 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
                             impl->s_out) != cudaSuccess)
             return 1;
     }
-    (void)used;
     if (cudaStreamSynchronize(impl->s_out) != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
         cudaGetLastError();
         return 1;
@@ -248,25 +310,32 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     }
     const float scale = norm_scale(h, backward_like);
     cudaStream_t st = h->stream;
-    const bool din = device_accessible(in), dout = device_accessible(out);
+    const Mem min = classify(in, dev), mout = classify(out, dev);
+    if (min == Mem::FOREIGN || mout == Mem::FOREIGN) {
+        gfft::set_last_error("a data pointer is device memory of another GPU than the current one");
+        return ACLFFT_INVALID_VALUE;
+    }
+    const bool din = min == Mem::DEVICE, dout = mout == Mem::DEVICE;
     if (din && dout) {
         const StepList& sl = (in == out) ? impl->lists[variant + 1] : primary;
         if (!sl.supported) return ACLFFT_NOT_IMPLEMENTED;
+        if (missing_workspace(impl, sl)) return no_workspace();
         return launch_list(impl, sl, in, out, st, c2c, inverse, scale) == 0 ? ACLFFT_SUCCESS : ACLFFT_EXEC_FAILED;
     }
     // host buffers: stage through device memory, return when done
+    if (missing_workspace(impl, primary)) return no_workspace();
     const size_t need = std::max(shape.in_bytes, shape.out_bytes);
     if (impl->stage_bytes < need) {
         if (impl->stage_a) cudaFree(impl->stage_a);
         if (impl->stage_b) cudaFree(impl->stage_b);
         impl->stage_a = impl->stage_b = nullptr;
         impl->stage_bytes = 0;
-        if (cudaMalloc(&impl->stage_a, need) != cudaSuccess || cudaMalloc(&impl->stage_b, need) != cudaSuccess) {
+        if (gfft::dev_alloc(&impl->stage_a, need) != cudaSuccess || gfft::dev_alloc(&impl->stage_b, need) != cudaSuccess) {
             cudaGetLastError();
             if (impl->stage_a) cudaFree(impl->stage_a);
             impl->stage_a = impl->stage_b = nullptr;
             gfft::set_last_error("cudaMalloc of the host staging buffers failed");
-            return ACLFFT_EXEC_FAILED;
+            return ACLFFT_ALLOC_FAILED;
         }
         impl->stage_bytes = need;
     }
@@ -275,7 +344,8 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     if (!din && !dout && primary.steps.size() == 1 && primary.steps[0].kind == Step::ROW) {
         const int rc = exec_host_pipelined(impl, primary.steps[0], in, out, shape.in_bytes, shape.out_bytes, st, c2c,
                                            inverse, scale);
-        if (rc >= 0) return rc == 0 ? ACLFFT_SUCCESS : ACLFFT_EXEC_FAILED;
+        if (rc > 0) return ACLFFT_EXEC_FAILED;
+        if (rc == 0) return drain_error_word(impl, st, nullptr);
     }
     if (!din && cudaMemcpyAsync(dev_in, in, shape.in_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         cudaGetLastError();
@@ -295,7 +365,9 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
         cudaGetLastError();
         return ACLFFT_EXEC_FAILED;
     }
-    return ACLFFT_SUCCESS;
+    // host buffers: the call has waited for the device anyway, so a wait
+    // that ran out is reported here
+    return drain_error_word(impl, st, nullptr);
 }
 
 size_t complex_elems(const aclfftHandle_t* h)
@@ -398,6 +470,36 @@ ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* id
     (void)idata;
     (void)odata;
     return ACLFFT_NOT_IMPLEMENTED;
+}
+
+ACLFFT_API aclfftResult aclfftGetExecError(aclfftHandle plan, int* flags)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(flags);
+    *flags = 0;
+    PlanImpl* impl = plan->impl;
+    if (!impl->device_ready || !impl->err) return ACLFFT_SUCCESS;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cur != impl->device) {
+        cudaGetLastError();
+        return ACLFFT_INVALID_DEVICE;
+    }
+    return drain_error_word(impl, plan->stream, flags);
+}
+
+ACLFFT_API aclfftResult aclfftDebugSetExecError(aclfftHandle plan, int flags)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    PlanImpl* impl = plan->impl;
+    if (!impl->device_ready || !impl->err) return ACLFFT_EXEC_FAILED;
+    if (cudaMemcpyAsync(impl->err, &flags, sizeof(int), cudaMemcpyHostToDevice, plan->stream) != cudaSuccess ||
+        cudaStreamSynchronize(plan->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    return ACLFFT_SUCCESS;
 }
 
 ACLFFT_API const char* aclfftGetLastErrorDetail(void) { return g_last_error.c_str(); }

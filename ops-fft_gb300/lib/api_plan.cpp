@@ -16,10 +16,10 @@
 // sequence, twiddles generated on the GPU, workspace), *workSize reports the
 // workspace the plan owns, and 2D plans accept any C2C size (the reference
 // only has {32,64,128}^2 kernels and returns ACLFFT_NOT_SUPPORTED otherwise).
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <new>
-
-#include <cstdlib>
 
 #include "handle.h"
 
@@ -83,11 +83,15 @@ aclfftResult check_sizes(const aclfftHandle_t* p)
     return ACLFFT_SUCCESS;
 }
 
-// Plans every call variant of the transform described by the handle.
-aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
+// Plans every call variant of the transform described by the handle on the
+// host (kernel steps, twiddle segments, workspace sizes); NULL on failure.
+PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
 {
     PlanImpl* impl = new (std::nothrow) PlanImpl();
-    if (!impl) return ACLFFT_ALLOC_FAILED;
+    if (!impl) {
+        *why = ACLFFT_ALLOC_FAILED;
+        return nullptr;
+    }
     Problem pr;
     pr.rank = h->rank;
     pr.kind = h->type == ACLFFT_C2C ? Kind::C2C : (h->type == ACLFFT_R2C ? Kind::R2C : Kind::C2R);
@@ -97,6 +101,7 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
     pr.stride = h->rank == 1 ? h->stride[0] : 1;
     pr.prec = pr.kind == Kind::C2C && pr.rank == 1 ? h->precision : 0;
     impl->prob = pr;
+    impl->auto_ws = h->auto_allocate;
     Problem adj = pr;
     if (pr.kind == Kind::R2C) {
         adj.kind = Kind::C2R;
@@ -115,8 +120,18 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
     if (!ok) {
         delete impl;
         gfft::set_last_error("internal planning failure");
-        return ACLFFT_INTERNAL_ERROR;
+        *why = ACLFFT_INTERNAL_ERROR;
+        return nullptr;
     }
+    return impl;
+}
+
+// Plans every call variant of the transform described by the handle.
+aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
+{
+    aclfftResult why = ACLFFT_SUCCESS;
+    PlanImpl* impl = plan_steps(h, &why);
+    if (!impl) return why;
     const aclfftResult r = gfft::plan_device_setup(impl);
     if (r != ACLFFT_SUCCESS) {
         gfft::plan_impl_free(impl);
@@ -124,11 +139,14 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
         return r;
     }
     if (h->impl) {  // re-plan of a made plan: the new state replaces the old
+        // a caller's work area stays bound when it is still large enough
+        if (!impl->auto_ws && h->impl->user_ws && gfft::work_area_bytes(impl) <= gfft::work_area_bytes(h->impl))
+            gfft::bind_work_area(impl, h->impl->user_ws);
         gfft::plan_impl_free(h->impl);
         delete h->impl;
     }
     h->impl = impl;
-    if (workSize) *workSize = (size_t)(impl->ws_bytes + impl->ws2_bytes);
+    if (workSize) *workSize = gfft::work_area_bytes(impl);
     return ACLFFT_SUCCESS;
 }
 
@@ -153,12 +171,64 @@ aclfftResult replan(aclfftHandle_t* h)
     return plan_execution(h, nullptr);
 }
 
+aclfftResult estimate_work_area(const aclfftHandle_t* desc, size_t* bytes)
+{
+    aclfftResult why = ACLFFT_SUCCESS;
+    PlanImpl* impl = plan_steps(desc, &why);
+    if (!impl) return why;
+    *bytes = work_area_bytes(impl);
+    delete impl;
+    return ACLFFT_SUCCESS;
+}
+
+size_t ws2_offset(const PlanImpl* p) { return ((size_t)p->ws_bytes + 255) & ~(size_t)255; }
+
+size_t work_area_bytes(const PlanImpl* p)
+{
+    return p->ws2_bytes > 0 ? ws2_offset(p) + (size_t)p->ws2_bytes : (size_t)p->ws_bytes;
+}
+
+void release_workspace(PlanImpl* p)
+{
+    if (!p->user_ws) {
+        if (p->ws) cudaFree(p->ws);
+        if (p->ws2) cudaFree(p->ws2);
+    }
+    p->ws = p->ws2 = p->user_ws = nullptr;
+}
+
+void bind_work_area(PlanImpl* p, void* area)
+{
+    release_workspace(p);
+    if (!area) return;
+    p->user_ws = area;
+    p->ws = p->ws_bytes > 0 ? area : nullptr;
+    p->ws2 = p->ws2_bytes > 0 ? static_cast<char*>(area) + ws2_offset(p) : nullptr;
+}
+
+aclfftResult allocate_workspace(PlanImpl* p)
+{
+    if (p->ws_bytes > 0 && dev_alloc(&p->ws, (size_t)p->ws_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p->ws = nullptr;
+        set_last_error("cudaMalloc of the workspace failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    if (p->ws2_bytes > 0 && dev_alloc(&p->ws2, (size_t)p->ws2_bytes) != cudaSuccess) {
+        cudaGetLastError();
+        p->ws2 = nullptr;
+        release_workspace(p);
+        set_last_error("cudaMalloc of the second workspace failed");
+        return ACLFFT_ALLOC_FAILED;
+    }
+    return ACLFFT_SUCCESS;
+}
+
 void plan_impl_free(PlanImpl* p)
 {
     if (!p) return;
     if (p->tw) cudaFree(p->tw);
-    if (p->ws) cudaFree(p->ws);
-    if (p->ws2) cudaFree(p->ws2);
+    release_workspace(p);
     if (p->stage_a) cudaFree(p->stage_a);
     if (p->stage_b) cudaFree(p->stage_b);
     if (p->err) cudaFree(p->err);
@@ -173,7 +243,7 @@ void plan_impl_free(PlanImpl* p)
         }
         p->pipe_ready = false;
     }
-    p->tw = p->ws = p->ws2 = p->stage_a = p->stage_b = nullptr;
+    p->tw = p->stage_a = p->stage_b = nullptr;
     p->device_ready = false;
 }
 
@@ -194,27 +264,21 @@ aclfftResult plan_device_setup(PlanImpl* p)
         return ACLFFT_SETUP_FAILED;
     }
     const size_t tw_bytes = (size_t)std::max<int64_t>(p->tb.count, 2) * 8;
-    if (cudaMalloc(&p->tw, tw_bytes) != cudaSuccess) {
+    if (dev_alloc(&p->tw, tw_bytes) != cudaSuccess) {
         cudaGetLastError();
         p->tw = nullptr;
         set_last_error("cudaMalloc of the twiddle table failed");
         return ACLFFT_ALLOC_FAILED;
     }
-    if (p->ws_bytes > 0 && cudaMalloc(&p->ws, (size_t)p->ws_bytes) != cudaSuccess) {
-        cudaGetLastError();
-        p->ws = nullptr;
-        plan_impl_free(p);
-        set_last_error("cudaMalloc of the workspace failed");
-        return ACLFFT_ALLOC_FAILED;
+    if (p->auto_ws && !p->user_ws) {
+        const aclfftResult r = allocate_workspace(p);
+        if (r != ACLFFT_SUCCESS) {
+            plan_impl_free(p);
+            return r;
+        }
     }
-    if (p->ws2_bytes > 0 && cudaMalloc(&p->ws2, (size_t)p->ws2_bytes) != cudaSuccess) {
-        cudaGetLastError();
-        p->ws2 = nullptr;
-        plan_impl_free(p);
-        set_last_error("cudaMalloc of the second workspace failed");
-        return ACLFFT_ALLOC_FAILED;
-    }
-    if (cudaMalloc(reinterpret_cast<void**>(&p->err), sizeof(int)) != cudaSuccess || cudaMemset(p->err, 0, sizeof(int)) != cudaSuccess) {
+    if (dev_alloc(reinterpret_cast<void**>(&p->err), sizeof(int)) != cudaSuccess ||
+        cudaMemset(p->err, 0, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         p->err = nullptr;
         plan_impl_free(p);
@@ -395,6 +459,127 @@ ACLFFT_API aclfftResult aclfftPlan3d(aclfftHandle* plan, int nx, int ny, int nz,
         *plan = nullptr;
     }
     return r;
+}
+
+// ------------------------------------------------------------ work area
+// The reference declares these and leaves them as stubs (lib/fft_utils_api.cpp:
+// 66-89); its roadmap describes them (docs/implementation.md:90-100,176-212):
+// query the work area a plan needs, let the plan allocate it (default) or
+// let the caller provide it.  Here the work area is the device scratch the
+// kernels use between passes (long 1D transforms split into column passes,
+// in-place calls whose rows change pitch, 2D transforms); many plans need
+// none.  Host-pointer execs additionally stage the data through plan-owned
+// buffers allocated at their first call; device-pointer execs never
+// allocate.
+
+ACLFFT_API aclfftResult aclfftGetSize1d(aclfftHandle plan, int nx, aclfftType type, int batch, size_t* workSize)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_NULL(workSize);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) return ACLFFT_NOT_SUPPORTED;
+    if (validate_1d_size(ACLFFT_HORIZONTAL, nx, "aclfftGetSize1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    aclfftHandle_t d;
+    d.rank = 1;
+    d.lengths[0] = nx;
+    d.stride[0] = 1;
+    d.batch = batch;
+    d.type = type;
+    d.precision = plan->precision;
+    if (check_sizes(&d) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    return gfft::estimate_work_area(&d, workSize);
+}
+
+ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclfftType type, size_t* workSize)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_NULL(workSize);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) return ACLFFT_NOT_SUPPORTED;
+    aclfftHandle_t d;
+    d.rank = 2;
+    d.lengths[0] = nx;
+    d.lengths[1] = ny;
+    d.stride[0] = d.stride[1] = 1;
+    d.batch = 1;
+    d.type = type;
+    if (check_sizes(&d) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    return gfft::estimate_work_area(&d, workSize);
+}
+
+ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
+                                        size_t* workSize)
+{
+    (void)plan; (void)nx; (void)ny; (void)nz; (void)type; (void)workSize;
+    return ACLFFT_NOT_IMPLEMENTED;  // no 3D transforms (aclfftMakePlan3d is a stub too)
+}
+
+ACLFFT_API aclfftResult aclfftGetSize(aclfftHandle plan, size_t* workSize)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_NULL(workSize);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    *workSize = gfft::work_area_bytes(plan->impl);
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftSetAutoAllocation(aclfftHandle plan, int autoAllocate)
+{
+    ACLFFT_CHECK_NULL(plan);
+    const bool on = autoAllocate != 0;
+    plan->auto_allocate = on;
+    PlanImpl* impl = plan->impl;
+    if (!plan->is_initialized || !impl || impl->auto_ws == on) {
+        if (impl) impl->auto_ws = on;
+        return ACLFFT_SUCCESS;
+    }
+    impl->auto_ws = on;
+    if (!on) {
+        // the plan's own workspace is released; a caller's area stays bound
+        if (!impl->user_ws) gfft::release_workspace(impl);
+        return ACLFFT_SUCCESS;
+    }
+    if (impl->user_ws || !impl->device_ready) return ACLFFT_SUCCESS;
+    const aclfftResult r = gfft::allocate_workspace(impl);
+    if (r != ACLFFT_SUCCESS) {
+        impl->auto_ws = false;
+        plan->auto_allocate = false;
+    }
+    return r;
+}
+
+ACLFFT_API aclfftResult aclfftSetWorkArea(aclfftHandle plan, void* workArea)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    PlanImpl* impl = plan->impl;
+    if (!workArea) {
+        // unbinds a caller's area; an auto-allocating plan gets its own back
+        gfft::bind_work_area(impl, nullptr);
+        if (impl->auto_ws && impl->device_ready) return gfft::allocate_workspace(impl);
+        return ACLFFT_SUCCESS;
+    }
+    if (reinterpret_cast<uintptr_t>(workArea) % 256 != 0) {
+        gfft::set_last_error("the work area must be 256-byte aligned");
+        return ACLFFT_UNALIGNED_DATA;
+    }
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, workArea) != cudaSuccess) {
+        cudaGetLastError();
+        at.type = cudaMemoryTypeUnregistered;
+    }
+    const bool ok = at.type == cudaMemoryTypeManaged ||
+                    (at.type == cudaMemoryTypeDevice && (!impl->device_ready || at.device == impl->device));
+    if (!ok) {
+        gfft::set_last_error("the work area must be device memory of the plan's device");
+        return ACLFFT_INVALID_VALUE;
+    }
+    gfft::bind_work_area(impl, workArea);
+    return ACLFFT_SUCCESS;
 }
 
 ACLFFT_API aclfftResult aclfftSetStream(aclfftHandle plan, cudaStream_t stream)

@@ -2,14 +2,35 @@
 // the GB300 extension getters/setters.
 //
 // aclfftGetErrorString follows lib/fft_utils_api.cpp:19-56 of the reference
-// (same strings, "Unknown error" otherwise); the work-area, stride and
-// version entries are stubs there too (lib/fft_utils_api.cpp:66-109).
+// (same strings, "Unknown error" otherwise).  The version queries are stubs
+// in the reference (lib/fft_utils_api.cpp:95-109) and its roadmap lists them
+// as library information (docs/implementation.md:101-106); here they report
+// this library's version.  aclfftSetStride stays a stub as in the reference
+// (lib/fft_utils_api.cpp:90-94).
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 
 #include "handle.h"
 
 namespace gfft {
+
+// Failure injection for device allocations: -1 off, k >= 0 lets k more
+// allocations succeed and fails every one after them.
+std::atomic<int> g_fail_alloc_after{-1};
+
+cudaError_t dev_alloc(void** p, size_t bytes)
+{
+    int k = g_fail_alloc_after.load();
+    while (k >= 0) {
+        if (k == 0) {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+        if (g_fail_alloc_after.compare_exchange_weak(k, k - 1)) break;
+    }
+    return cudaMalloc(p, bytes);
+}
 
 bool log_enabled()
 {
@@ -47,43 +68,6 @@ ACLFFT_API const char* aclfftGetErrorString(aclfftResult result)
     }
 }
 
-ACLFFT_API aclfftResult aclfftGetSize1d(aclfftHandle plan, int nx, aclfftType type, int batch, size_t* workSize)
-{
-    (void)plan; (void)nx; (void)type; (void)batch; (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
-ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclfftType type, size_t* workSize)
-{
-    (void)plan; (void)nx; (void)ny; (void)type; (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
-ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
-                                        size_t* workSize)
-{
-    (void)plan; (void)nx; (void)ny; (void)nz; (void)type; (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
-ACLFFT_API aclfftResult aclfftGetSize(aclfftHandle plan, size_t* workSize)
-{
-    (void)plan; (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
-ACLFFT_API aclfftResult aclfftSetAutoAllocation(aclfftHandle plan, int autoAllocate)
-{
-    (void)plan; (void)autoAllocate;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
-ACLFFT_API aclfftResult aclfftSetWorkArea(aclfftHandle plan, void* workArea)
-{
-    (void)plan; (void)workArea;
-    return ACLFFT_NOT_IMPLEMENTED;
-}
-
 ACLFFT_API aclfftResult aclfftSetStride(aclfftHandle plan, int32_t stride)
 {
     (void)plan; (void)stride;
@@ -92,14 +76,26 @@ ACLFFT_API aclfftResult aclfftSetStride(aclfftHandle plan, int32_t stride)
 
 ACLFFT_API aclfftResult aclfftGetVersion(int* version)
 {
-    (void)version;
-    return ACLFFT_NOT_IMPLEMENTED;
+    ACLFFT_CHECK_NULL(version);
+    *version = ACLFFT_GB300_VERSION;
+    return ACLFFT_SUCCESS;
 }
 
 ACLFFT_API aclfftResult aclfftGetProperty(aclfftLibraryPropertyType type, int* value)
 {
-    (void)type; (void)value;
-    return ACLFFT_NOT_IMPLEMENTED;
+    ACLFFT_CHECK_NULL(value);
+    switch (type) {
+    case ACLFFT_MAJOR_VERSION: *value = ACLFFT_GB300_VERSION_MAJOR; return ACLFFT_SUCCESS;
+    case ACLFFT_MINOR_VERSION: *value = ACLFFT_GB300_VERSION_MINOR; return ACLFFT_SUCCESS;
+    case ACLFFT_PATCH_LEVEL: *value = ACLFFT_GB300_VERSION_PATCH; return ACLFFT_SUCCESS;
+    default: return ACLFFT_INVALID_TYPE;
+    }
+}
+
+ACLFFT_API aclfftResult aclfftDebugFailAllocations(int after)
+{
+    gfft::g_fail_alloc_after.store(after < 0 ? -1 : after);
+    return ACLFFT_SUCCESS;
 }
 
 // ------------------------------------------------------------- extensions
@@ -194,7 +190,24 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
         break;
     }
     info->twiddle_entries = plan->impl->tb.count;
-    info->workspace_bytes = (size_t)(plan->impl->ws_bytes + plan->impl->ws2_bytes);
+    info->workspace_bytes = gfft::work_area_bytes(plan->impl);
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftDebugGetTwiddleSegments(aclfftHandle plan, long long* segs, int maxSegs, int* nsegs)
+{
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(plan->is_initialized && plan->impl, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_NULL(nsegs);
+    const auto& v = plan->impl->tb.segs;
+    *nsegs = (int)v.size();
+    for (int i = 0; segs && i < maxSegs && i < (int)v.size(); ++i) {
+        segs[5 * i + 0] = v[i].offset;
+        segs[5 * i + 1] = v[i].count;
+        segs[5 * i + 2] = v[i].M;
+        segs[5 * i + 3] = v[i].R_or_mult;
+        segs[5 * i + 4] = v[i].kind;
+    }
     return ACLFFT_SUCCESS;
 }
 

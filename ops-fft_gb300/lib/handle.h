@@ -34,6 +34,11 @@ struct PlanImpl {
     void* tw = nullptr;
     void* ws = nullptr;
     void* ws2 = nullptr;
+    // workspace ownership: with auto allocation (the default) the plan
+    // allocates ws/ws2 itself; otherwise they point into the caller's work
+    // area (aclfftSetWorkArea), or are NULL until one is set
+    bool auto_ws = true;
+    void* user_ws = nullptr;
     int* err = nullptr;  // device error word written by bounded waits
     // host staging (allocated on the first exec with host pointers)
     void* stage_a = nullptr;
@@ -57,6 +62,23 @@ aclfftResult plan_device_setup(PlanImpl* p);
 void set_last_error(const std::string& s);
 bool log_enabled();
 
+// cudaMalloc behind a failure-injection hook (aclfftDebugFailAllocations):
+// every device allocation of the library goes through here.
+cudaError_t dev_alloc(void** p, size_t bytes);
+
+// Bytes of the caller-provided work area a plan needs: ws, then ws2 at a
+// 256-byte aligned offset.
+size_t work_area_bytes(const PlanImpl* p);
+size_t ws2_offset(const PlanImpl* p);
+// Points the plan's workspaces into a caller-owned area (NULL unbinds),
+// freeing any workspace the plan allocated itself.
+void bind_work_area(PlanImpl* p, void* area);
+void release_workspace(PlanImpl* p);
+aclfftResult allocate_workspace(PlanImpl* p);
+// Work area of a transform description without creating any device state
+// (aclfftGetSize1d/2d).
+aclfftResult estimate_work_area(const aclfftHandle_t* desc, size_t* bytes);
+
 }  // namespace gfft
 
 struct aclfftHandle_t {
@@ -69,11 +91,12 @@ struct aclfftHandle_t {
     cudaStream_t stream;
     bool is_initialized;
     gfft::PlanImpl* impl;
-    int32_t precision;  // aclfftPrecisionMode (extension)
+    int32_t precision;    // aclfftPrecisionMode (extension)
+    bool auto_allocate;   // aclfftSetAutoAllocation (default: the plan allocates its workspace)
 
     aclfftHandle_t()
         : rank(0), lengths{0, 0, 0}, stride{0, 0, 0}, batch(1), type(ACLFFT_C2C), normMode(0), stream(nullptr),
-          is_initialized(false), impl(nullptr), precision(0)
+          is_initialized(false), impl(nullptr), precision(0), auto_allocate(true)
     {
     }
     ~aclfftHandle_t()

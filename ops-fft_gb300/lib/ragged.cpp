@@ -159,6 +159,8 @@ struct aclfftRaggedPlan_t {
     int nlong = 0;
     int64_t in_min = 0, out_min = 0;
     bool autotune = true, use_graph = true, tuned = false;
+    long long wait_cycles = 1ll << 31;  // bound of each dependency wait
+    int need_bias = 0;                  // test hook: unreachable dependency counts
     cudaStream_t stream = nullptr;
     // device state
     bool dev_ready = false;
@@ -202,6 +204,16 @@ void free_device(aclfftRaggedPlan_t* p)
 }
 
 int ctas_for(aclfftRaggedPlan_t* p, int smem);
+
+// The captured graph bakes in the kernel arguments: settings that change
+// them force a new capture at the next exec.
+void drop_graph(aclfftRaggedPlan_t* p)
+{
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    p->gexec = nullptr;
+    p->g_in = p->g_out = nullptr;
+    p->g_inv = -1;
+}
 
 // Shared memory an item of the class needs with the chosen variants: the
 // data buffers, then the staged pass-table window.
@@ -342,7 +354,7 @@ bool upload(T*& d, const std::vector<T>& h)
     if (d) cudaFree(d);
     d = nullptr;
     const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
-    if (cudaMalloc(reinterpret_cast<void**>(&d), bytes) != cudaSuccess) {
+    if (gfft::dev_alloc(reinterpret_cast<void**>(&d), bytes) != cudaSuccess) {
         cudaGetLastError();
         d = nullptr;
         return false;
@@ -371,12 +383,12 @@ aclfftResult device_setup(aclfftRaggedPlan_t* p)
         return ACLFFT_SETUP_FAILED;
     }
     const size_t twb = (size_t)std::max<int64_t>(p->tb.count, 2) * 8;
-    if (cudaMalloc(&p->tw, twb) != cudaSuccess || cudaMalloc(reinterpret_cast<void**>(&p->d_queue),
+    if (gfft::dev_alloc(&p->tw, twb) != cudaSuccess || gfft::dev_alloc(reinterpret_cast<void**>(&p->d_queue),
                                                              (size_t)(p->count + 1) * sizeof(int)) != cudaSuccess ||
-        cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)) != cudaSuccess ||
+        gfft::dev_alloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)) != cudaSuccess ||
         cudaMemset(p->d_err, 0, sizeof(int)) != cudaSuccess ||
         (p->ws_floats2 > 0 &&
-         cudaMalloc(reinterpret_cast<void**>(&p->d_ws), (size_t)p->ws_floats2 * sizeof(float2)) != cudaSuccess) ||
+         gfft::dev_alloc(reinterpret_cast<void**>(&p->d_ws), (size_t)p->ws_floats2 * sizeof(float2)) != cudaSuccess) ||
         cudaStreamCreateWithFlags(&p->s_cap, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         free_device(p);
@@ -443,6 +455,8 @@ RagArgs make_args(aclfftRaggedPlan_t* p, const RagItem* items, int nitems, int s
     a.ws = p->d_ws;
     a.inverse = inverse ? 1 : 0;
     a.scale_c2c = 1.f;
+    a.wait_cycles = p->wait_cycles;
+    a.need_bias = p->need_bias;
     return a;
 }
 
@@ -484,10 +498,10 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
     RagItem* sitems = nullptr;
     RagClass* scls = nullptr;
     size_t cap_xf = 0, cap_order = 0, cap_items = 0, cap_cls = 0;
-    bool ok = cudaMalloc(&sin, (size_t)scratch) == cudaSuccess && cudaMalloc(&sout, (size_t)scratch) == cudaSuccess &&
+    bool ok = gfft::dev_alloc(&sin, (size_t)scratch) == cudaSuccess && gfft::dev_alloc(&sout, (size_t)scratch) == cudaSuccess &&
               cudaMemset(sin, 0, (size_t)scratch) == cudaSuccess &&
-              cudaMalloc(reinterpret_cast<void**>(&squeue), (size_t)(maxm + 1) * sizeof(int)) == cudaSuccess &&
-              cudaMalloc(reinterpret_cast<void**>(&sws), (size_t)wsmax * sizeof(float2)) == cudaSuccess;
+              gfft::dev_alloc(reinterpret_cast<void**>(&squeue), (size_t)(maxm + 1) * sizeof(int)) == cudaSuccess &&
+              gfft::dev_alloc(reinterpret_cast<void**>(&sws), (size_t)wsmax * sizeof(float2)) == cudaSuccess;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
     for (int ci = 0; ci < (int)p->classes.size() && ok; ++ci) {
@@ -530,7 +544,7 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
                         if (d) cudaFree(d);
                         d = nullptr;
                         cap = 0;
-                        if (cudaMalloc(reinterpret_cast<void**>(&d), h.size() * sizeof(T)) != cudaSuccess) return false;
+                        if (gfft::dev_alloc(reinterpret_cast<void**>(&d), h.size() * sizeof(T)) != cudaSuccess) return false;
                         cap = h.size();
                     }
                     return h.empty() ||
@@ -556,6 +570,8 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
                 ra.out = sout;
                 ra.ws = sws;
                 ra.scale_c2c = 1.f;
+                ra.wait_cycles = 1ll << 31;  // trials never use the plan's test settings
+                ra.need_bias = 0;
                 if (ra.ctas <= 0) {
                     ok = false;
                     break;
@@ -609,14 +625,17 @@ aclfftResult autotune(aclfftRaggedPlan_t* p)
     return ACLFFT_SUCCESS;
 }
 
-bool device_pointer(const void* ptr)
+// Device memory of device `dev` (any device when dev < 0) or managed
+// memory; another GPU's memory would be dereferenced as a peer address.
+bool device_pointer(const void* ptr, int dev)
 {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+    if (at.type == cudaMemoryTypeManaged) return true;
+    return at.type == cudaMemoryTypeDevice && (dev < 0 || at.device == dev);
 }
 
 }  // namespace
@@ -771,7 +790,7 @@ ACLFFT_API aclfftResult aclfftRaggedExec(aclfftRaggedPlan plan, void* idata, voi
     ACLFFT_CHECK_NULL(idata);
     ACLFFT_CHECK_NULL(odata);
     ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
-    if (!device_pointer(idata) || !device_pointer(odata)) {
+    if (!device_pointer(idata, -1) || !device_pointer(odata, -1)) {
         gfft::set_last_error("ragged exec takes device pointers");
         return ACLFFT_INVALID_VALUE;
     }
@@ -781,6 +800,10 @@ ACLFFT_API aclfftResult aclfftRaggedExec(aclfftRaggedPlan plan, void* idata, voi
     if (cudaGetDevice(&dev) != cudaSuccess || dev != plan->device) {
         cudaGetLastError();
         return ACLFFT_INVALID_DEVICE;
+    }
+    if (!device_pointer(idata, dev) || !device_pointer(odata, dev)) {
+        gfft::set_last_error("ragged exec takes device pointers of the plan's device");
+        return ACLFFT_INVALID_VALUE;
     }
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(plan->stream, &cs) != cudaSuccess) {
@@ -852,10 +875,40 @@ ACLFFT_API aclfftResult aclfftRaggedGetError(aclfftRaggedPlan plan, int* flags)
     ACLFFT_CHECK_NULL(flags);
     *flags = 0;
     if (!plan->dev_ready) return ACLFFT_SUCCESS;
-    if (cudaMemcpy(flags, plan->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    // ordered after the plan's launches: the read is queued on the plan's
+    // stream (which may be a non-blocking stream the legacy default stream
+    // does not wait for) and that stream is synchronised
+    int v = 0;
+    if (cudaMemcpyAsync(&v, plan->d_err, sizeof(int), cudaMemcpyDeviceToHost, plan->stream) != cudaSuccess ||
+        cudaStreamSynchronize(plan->stream) != cudaSuccess) {
         cudaGetLastError();
+        gfft::set_last_error("ragged: reading the device error word failed");
         return ACLFFT_EXEC_FAILED;
     }
+    *flags = v;
+    if (v == 0) return ACLFFT_SUCCESS;
+    if (cudaMemsetAsync(plan->d_err, 0, sizeof(int), plan->stream) != cudaSuccess ||
+        cudaStreamSynchronize(plan->stream) != cudaSuccess)
+        cudaGetLastError();
+    gfft::set_last_error("ragged: a dependency wait ran out of time; the output is incomplete");
+    return ACLFFT_EXEC_FAILED;
+}
+
+ACLFFT_API aclfftResult aclfftRaggedSetWaitLimit(aclfftRaggedPlan plan, long long cycles)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_PARAM(cycles > 0, ACLFFT_INVALID_VALUE);
+    if (plan->wait_cycles != cycles) drop_graph(plan);
+    plan->wait_cycles = cycles;
+    return ACLFFT_SUCCESS;
+}
+
+ACLFFT_API aclfftResult aclfftRaggedDebugHoldDependencies(aclfftRaggedPlan plan, int extra)
+{
+    ACLFFT_CHECK_PARAM(plan != nullptr, ACLFFT_INVALID_PLAN);
+    ACLFFT_CHECK_PARAM(extra >= 0, ACLFFT_INVALID_VALUE);
+    if (plan->need_bias != extra) drop_graph(plan);
+    plan->need_bias = extra;
     return ACLFFT_SUCCESS;
 }
 

@@ -6,7 +6,10 @@
     Z = F.fft(z, inverse=False)
 
 Every forward and backward call is one aclfftExec* / aclfftExec*Adjoint call
-on the current torch stream; plans are cached per (kind, n, batch, device).
+on the current torch stream.  Plans are cached per (kind, n, batch, device,
+stream): a plan's stream and workspace are never shared by two streams, and
+a per-plan lock serialises the host-side calls of threads that share a
+stream (a plan is not thread-safe).
 Gradients follow torch's complex convention (dL/dRe + i dL/dIm): the
 backward of fft is the opposite-direction transform, the backward of rfft is
 the R2C adjoint (C2R of the gradient with interior bins halved) and the
@@ -25,21 +28,31 @@ _plans = {}
 _lock = threading.Lock()
 
 
-def _plan(kind: int, n: int, batch: int, device: torch.device) -> A.Plan:
-    key = (kind, n, batch, device.index)
+def _plan(kind: int, n: int, batch: int, device: torch.device):
+    """The cached plan for this shape on the current stream of `device`, and
+    the lock that guards its use."""
+    stream = torch.cuda.current_stream(device)
+    key = (kind, n, batch, device.index, stream.cuda_stream)
     with _lock:
-        p = _plans.get(key)
-        if p is None:
+        entry = _plans.get(key)
+        if entry is None:
             with torch.cuda.device(device):
                 p = A.Plan.plan1d(n, kind, batch)
-            _plans[key] = p
-    p.set_stream(torch.cuda.current_stream(device))
-    return p
+            p.set_stream(stream)  # bound once: the key includes the stream
+            entry = (p, threading.Lock())
+            _plans[key] = entry
+    return entry
+
+
+def _run(kind: int, n: int, batch: int, device: torch.device, method: str, *args) -> None:
+    p, plock = _plan(kind, n, batch, device)
+    with plock:
+        getattr(p, method)(*args)
 
 
 def clear_cache() -> None:
     with _lock:
-        for p in _plans.values():
+        for p, _ in _plans.values():
             p.destroy()
         _plans.clear()
 
@@ -58,7 +71,7 @@ class _C2C(torch.autograd.Function):
         n = x.shape[-1]
         x, b = _rows(x.to(torch.complex64), n)
         y = torch.empty_like(x)
-        _plan(A.C2C, n, b, x.device).exec_c2c(x, y, A.BACKWARD if inverse else A.FORWARD)
+        _run(A.C2C, n, b, x.device, "exec_c2c", x, y, A.BACKWARD if inverse else A.FORWARD)
         ctx.inverse = inverse
         return y
 
@@ -67,7 +80,7 @@ class _C2C(torch.autograd.Function):
         n = g.shape[-1]
         g, b = _rows(g.to(torch.complex64), n)
         gx = torch.empty_like(g)
-        _plan(A.C2C, n, b, g.device).exec_c2c_adjoint(g, gx, A.BACKWARD if ctx.inverse else A.FORWARD)
+        _run(A.C2C, n, b, g.device, "exec_c2c_adjoint", g, gx, A.BACKWARD if ctx.inverse else A.FORWARD)
         return gx, None
 
 
@@ -77,7 +90,7 @@ class _R2C(torch.autograd.Function):
         n = x.shape[-1]
         x, b = _rows(x.to(torch.float32), n)
         out = torch.empty(x.shape[:-1] + (n // 2 + 1,), dtype=torch.complex64, device=x.device)
-        _plan(A.R2C, n, b, x.device).exec_r2c(x, out)
+        _run(A.R2C, n, b, x.device, "exec_r2c", x, out)
         ctx.n = n
         return out
 
@@ -86,7 +99,7 @@ class _R2C(torch.autograd.Function):
         n = ctx.n
         g, b = _rows(g.to(torch.complex64), n // 2 + 1)
         gx = torch.empty(g.shape[:-1] + (n,), dtype=torch.float32, device=g.device)
-        _plan(A.R2C, n, b, g.device).exec_r2c_adjoint(g, gx)
+        _run(A.R2C, n, b, g.device, "exec_r2c_adjoint", g, gx)
         return gx
 
 
@@ -95,7 +108,7 @@ class _C2R(torch.autograd.Function):
     def forward(ctx, X: torch.Tensor, n: int):
         X, b = _rows(X.to(torch.complex64), n // 2 + 1)
         out = torch.empty(X.shape[:-1] + (n,), dtype=torch.float32, device=X.device)
-        _plan(A.C2R, n, b, X.device).exec_c2r(X, out)
+        _run(A.C2R, n, b, X.device, "exec_c2r", X, out)
         ctx.n = n
         return out
 
@@ -104,7 +117,7 @@ class _C2R(torch.autograd.Function):
         n = ctx.n
         g, b = _rows(g.to(torch.float32), n)
         gX = torch.empty(g.shape[:-1] + (n // 2 + 1,), dtype=torch.complex64, device=g.device)
-        _plan(A.C2R, n, b, g.device).exec_c2r_adjoint(g, gX)
+        _run(A.C2R, n, b, g.device, "exec_c2r_adjoint", g, gX)
         return gX, None
 
 

@@ -157,25 +157,99 @@ def test_makeplan_twice_and_create_null():
 
 
 def test_stubs_return_not_implemented():
+    """Entries that stay stubs, as in the reference (lib/fft_utils_api.cpp,
+    lib/fft_exec_api.cpp:87-116): 3D, double precision and SetStride."""
     mine = A.lib()
     h = ctypes.c_void_p()
     sz = ctypes.c_size_t()
-    v = ctypes.c_int()
-    assert mine.aclfftGetSize1d(h, 8, A.C2C, 1, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
-    assert mine.aclfftGetSize2d(h, 8, 8, A.C2C, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
     assert mine.aclfftGetSize3d(h, 8, 8, 8, A.C2C, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
-    assert mine.aclfftGetSize(h, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
-    assert mine.aclfftSetAutoAllocation(h, 1) == A.NOT_IMPLEMENTED
-    assert mine.aclfftSetWorkArea(h, None) == A.NOT_IMPLEMENTED
     assert mine.aclfftSetStride(h, 2) == A.NOT_IMPLEMENTED
-    assert mine.aclfftGetVersion(ctypes.byref(v)) == A.NOT_IMPLEMENTED
-    assert mine.aclfftGetProperty(0, ctypes.byref(v)) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecZ2Z(h, None, None, -1) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecD2Z(h, None, None) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecZ2D(h, None, None) == A.NOT_IMPLEMENTED
     hp = ctypes.c_void_p()
     assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, A.C2C) == A.NOT_IMPLEMENTED
     assert not hp.value
+
+
+def test_version_queries():
+    """aclfftGetVersion / aclfftGetProperty (stubs in the reference,
+    lib/fft_utils_api.cpp:95-109) report this library's version."""
+    mine = A.lib()
+    v = ctypes.c_int()
+    assert mine.aclfftGetVersion(None) == A.INVALID_VALUE
+    assert mine.aclfftGetVersion(ctypes.byref(v)) == A.SUCCESS
+    parts = []
+    for prop in (0, 1, 2):
+        x = ctypes.c_int(-1)
+        assert mine.aclfftGetProperty(prop, ctypes.byref(x)) == A.SUCCESS
+        parts.append(x.value)
+    assert v.value == parts[0] * 10000 + parts[1] * 100 + parts[2]
+    assert mine.aclfftGetProperty(3, ctypes.byref(v)) == A.INVALID_TYPE
+    assert mine.aclfftGetProperty(0, None) == A.INVALID_VALUE
+
+
+def test_work_area_queries():
+    """aclfftGetSize1d/2d estimate the work area without creating device
+    state and agree with aclfftGetSize / MakePlan's *workSize of the made
+    plan; argument checks follow MakePlan's."""
+    mine = A.lib()
+    h = ctypes.c_void_p()
+    assert mine.aclfftCreate(ctypes.byref(h)) == 0
+    sz = ctypes.c_size_t()
+    assert mine.aclfftGetSize1d(None, 64, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_VALUE
+    assert mine.aclfftGetSize1d(h, 64, A.C2C, 1, None) == A.INVALID_VALUE
+    assert mine.aclfftGetSize1d(h, 0, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_SIZE
+    assert mine.aclfftGetSize1d(h, 64, A.C2C, 0, ctypes.byref(sz)) == A.INVALID_SIZE
+    assert mine.aclfftGetSize1d(h, 64, 0x2B, 1, ctypes.byref(sz)) == A.INVALID_TYPE
+    assert mine.aclfftGetSize1d(h, 64, A.Z2Z, 1, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize1d(h, (1 << 27) + 1, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_SIZE
+    assert mine.aclfftGetSize2d(h, 64, 64, A.R2C, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize(h, ctypes.byref(sz)) == A.INVALID_PLAN  # not made yet
+    mine.aclfftDestroy(h)
+    cases = [(4096, A.C2C, 256), (3000, A.R2C, 4096), (1024, A.C2R, 16), (1 << 20, A.C2C, 4), (1 << 25, A.R2C, 2),
+             (46200, A.C2C, 3), (999, A.R2C, 5)]
+    for n, t, b in cases:
+        est = ctypes.c_size_t()
+        made = ctypes.c_size_t()
+        q = ctypes.c_void_p()
+        assert mine.aclfftCreate(ctypes.byref(q)) == 0
+        assert mine.aclfftGetSize1d(q, n, t, b, ctypes.byref(est)) == 0
+        assert mine.aclfftMakePlan1d(q, n, t, b, 0, ctypes.byref(made)) == 0
+        assert mine.aclfftGetSize(q, ctypes.byref(sz)) == 0
+        assert est.value == made.value == sz.value, (n, t, b, est.value, made.value, sz.value)
+        mine.aclfftDestroy(q)
+    for nx, ny in ((2048, 2048), (64, 128), (7, 3000)):
+        est = ctypes.c_size_t()
+        with A.Plan.plan2d(1, nx, ny, A.C2C) as p:
+            assert mine.aclfftGetSize2d(p.handle, nx, ny, A.C2C, ctypes.byref(est)) == 0
+            assert est.value == p.work_size()
+    # a long transform needs a work area between its passes
+    with A.Plan.plan1d(1 << 20, A.C2C, 4) as p:
+        assert p.work_size() > 0
+
+
+def test_auto_allocation_and_work_area_contract():
+    """SetAutoAllocation before MakePlan is recorded; SetWorkArea needs a
+    made plan, a 256-byte aligned pointer and device memory (host memory is
+    refused; no device is needed to check that)."""
+    mine = A.lib()
+    assert mine.aclfftSetAutoAllocation(None, 0) == A.INVALID_VALUE
+    h = ctypes.c_void_p()
+    assert mine.aclfftCreate(ctypes.byref(h)) == 0
+    assert mine.aclfftSetWorkArea(h, None) == A.INVALID_PLAN
+    assert mine.aclfftSetAutoAllocation(h, 0) == 0
+    ws = ctypes.c_size_t()
+    assert mine.aclfftMakePlan1d(h, 1 << 20, A.C2C, 2, 0, ctypes.byref(ws)) == 0
+    assert ws.value > 0
+    host = np.zeros(ws.value // 4 + 64, dtype=np.float32)
+    addr = host.ctypes.data
+    aligned = (addr + 255) // 256 * 256
+    assert mine.aclfftSetWorkArea(h, aligned + 8) == A.UNALIGNED_DATA
+    assert mine.aclfftSetWorkArea(h, aligned) == A.INVALID_VALUE
+    assert mine.aclfftSetWorkArea(h, None) == 0
+    assert mine.aclfftSetAutoAllocation(h, 1) == 0
+    assert mine.aclfftDestroy(h) == 0
 
 
 def test_error_strings_match_reference():

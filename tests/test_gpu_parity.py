@@ -57,11 +57,16 @@ def _fft1_case_io(c):
     return n, b, x, gold
 
 
-@pytest.mark.parametrize("c", cases("fft1_d", include_skipped=True), ids=lambda c: c["name"])
+def _small(op):
+    return [c for c in cases(op, include_skipped=True) if c["n"] * c["batch"] <= MAX_REGEN_ELEMS]
+
+
+def _large(op):
+    return [c for c in cases(op, include_skipped=True) if c["n"] * c["batch"] > MAX_REGEN_ELEMS]
+
+
+@pytest.mark.parametrize("c", _small("fft1_d"), ids=lambda c: c["name"])
 def test_fft1_d_reference_cases(c):
-    n, b = c["n"], c["batch"]
-    if n * b > MAX_REGEN_ELEMS:
-        pytest.skip("larger than the regenerated-case cap")
     n, b, x, gold = _fft1_case_io(c)
     if c.get("roundtrip"):
         mid = c2c_host(n, b, x, A.FORWARD)
@@ -81,11 +86,9 @@ def test_fft1_d_reference_cases(c):
     _fp64_ok(out, exact, what=c["name"])
 
 
-@pytest.mark.parametrize("c", cases("rfft1_d", include_skipped=True), ids=lambda c: c["name"])
+@pytest.mark.parametrize("c", _small("rfft1_d"), ids=lambda c: c["name"])
 def test_rfft1_d_reference_cases(c):
     n, b = c["n"], c["batch"]
-    if n * b > MAX_REGEN_ELEMS:
-        pytest.skip("larger than the regenerated-case cap")
     if "files" in c:
         x = read_bin("rfft1_d", c["files"]["input"]).copy()
         gold = read_bin("rfft1_d", c["files"]["golden"])
@@ -128,6 +131,83 @@ def test_fft2_d_reference_cases(c):
         p.exec_c2c(x, out, d)
     _gold_ok(out, gold, c)
     _fp64_ok(out, O.c2c_2d(x.reshape(b, nx, ny), d), what=c["name"])
+
+
+# ----------------------------------------- the reference's largest cases
+# Cases above 2^26 elements (R2C up to N = 2^27, the 263168-column VERTICAL
+# case) run at the reference's full shape on device buffers.  Inputs follow
+# the reference recipe's distribution (randn, seeded) but are drawn on the
+# GPU; the FP64 oracle checks sampled transforms with the reference's own
+# atol/rtol and the FP32 bound, and a size-independent property covers every
+# transform: the unnormalised round trip returns n * x.
+def _rel_diff_chunked(a, b, scale, rows_per_chunk):
+    """||a - scale*b|| / ||scale*b|| over rows, in float64, chunked."""
+    num = den = 0.0
+    for r0 in range(0, a.shape[0], rows_per_chunk):
+        ad = a[r0: r0 + rows_per_chunk].double()
+        bd = b[r0: r0 + rows_per_chunk].double() * scale
+        num += float(torch.sum((ad - bd) ** 2))
+        den += float(torch.sum(bd ** 2))
+    return (num / den) ** 0.5
+
+
+@pytest.mark.parametrize("c", _large("rfft1_d"), ids=lambda c: c["name"])
+def test_rfft1_d_large_reference_cases_full_shape(c):
+    n, b = c["n"], c["batch"]
+    dev = _dev()
+    g = torch.Generator(device=dev).manual_seed(12345)
+    x = torch.randn((b, n), generator=g, device=dev)
+    X = torch.empty((b, n // 2 + 1), dtype=torch.complex64, device=dev)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_r2c(x, X)
+        torch.cuda.synchronize()
+        assert p.exec_error() == 0
+    rows = sorted({0, b - 1}) if n <= (1 << 22) else [b - 1]
+    for r in rows:
+        xr = x[r].cpu().numpy()
+        exact = O.r2c(xr[None, :])[0] if n <= (1 << 22) else O.r2c_long_rows(xr)
+        out = X[r].cpu().numpy()
+        ok, det = O.comparison_details(out, exact, c["atol"], c["rtol"])
+        assert ok, (c["name"], r, det)
+        _fp64_ok(out, exact, what=(c["name"], r))
+        assert out[0].imag == 0 and out[-1].imag == 0
+    y = torch.empty_like(x)
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2r(X, y)
+        torch.cuda.synchronize()
+        assert p.exec_error() == 0
+    rel = _rel_diff_chunked(y, x, float(n), max(1, (1 << 24) // n))
+    assert rel <= REL_FP32, (c["name"], "round trip", rel)
+
+
+@pytest.mark.parametrize("c", _large("fft1_d"), ids=lambda c: c["name"])
+def test_fft1_d_large_reference_cases_full_shape(c):
+    n, b = c["n"], c["batch"]
+    assert c.get("vertical")
+    dev = _dev()
+    g = torch.Generator(device=dev).manual_seed(12345)
+    x = torch.complex(torch.randn((n, b), generator=g, device=dev), torch.randn((n, b), generator=g, device=dev))
+    y = torch.empty_like(x)
+    d = A.FORWARD if c["forward"] else A.BACKWARD
+    with A.Plan.plan1d(n, A.C2C, b, A.VERTICAL) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2c(x, y, d)
+        torch.cuda.synchronize()
+        cols = np.unique(np.concatenate([np.arange(8), np.linspace(0, b - 1, 56).astype(np.int64)]))
+        xs = x[:, cols].cpu().numpy()
+        exact = O.c2c_vertical(xs, d)
+        out = y[:, cols].cpu().numpy()
+        ok, det = O.comparison_details(out, exact, c["atol"], c["rtol"])
+        assert ok, (c["name"], det)
+        _fp64_ok(out, exact, what=c["name"])
+        z = torch.empty_like(x)
+        p.exec_c2c(y, z, -d)
+        torch.cuda.synchronize()
+        assert p.exec_error() == 0
+    rel = _rel_diff_chunked(torch.view_as_real(z), torch.view_as_real(x), float(n), 16)
+    assert rel <= REL_FP32, (c["name"], "round trip", rel)
 
 
 # --------------------------------------------------- BASELINE configurations
@@ -322,6 +402,33 @@ def test_r2c_c2r_inplace_device(n):
     _fp64_ok(y, n * x.astype(np.float64), what=("c2r in place", n))
 
 
+@pytest.mark.parametrize("n,b", [(1024, 4096), (3000, 4096), (1025, 64), (1 << 20, 2)])
+def test_host_inplace_r2c_c2r_c2c(n, b):
+    """In-place calls on HOST buffers (the reference's documented layout,
+    docs/zh/API_Reference/FFT_1D.md:201: one buffer of batch*2*(n/2+1)
+    floats, the input rows packed at its start).  The batch-4096 shapes are
+    large enough to take the chunked host pipeline, where an R2C chunk's
+    output rows cover later chunks' input rows."""
+    rng = np.random.default_rng(n + b)
+    x = rng.standard_normal((b, n)).astype(np.float32)
+    buf = np.zeros(b * 2 * (n // 2 + 1), dtype=np.float32)
+    buf[: b * n] = x.reshape(-1)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.exec_r2c(buf, buf)
+    X = buf.view(np.complex64).reshape(b, n // 2 + 1).copy()
+    _fp64_ok(X, O.r2c(x), what=("host r2c in place", n, b))
+    with A.Plan.plan1d(n, A.C2R, b) as p:
+        p.exec_c2r(buf, buf)
+    y = buf[: b * n].reshape(b, n)
+    _fp64_ok(y, O.c2r(X, n), what=("host c2r in place", n, b))
+    _fp64_ok(y, n * x.astype(np.float64), what=("host round trip in place", n, b))
+    z = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
+    zb = z.reshape(-1).copy()
+    with A.Plan.plan1d(n, A.C2C, b) as p:
+        p.exec_c2c(zb, zb, A.FORWARD)
+    _fp64_ok(zb.reshape(b, n), O.c2c(z, -1), what=("host c2c in place", n, b))
+
+
 @pytest.mark.parametrize("mode", [A.NORM_NONE, A.NORM_BACKWARD, A.NORM_ORTHO, A.NORM_FORWARD])
 def test_norm_modes(mode):
     n, b = 1000, 3
@@ -446,14 +553,48 @@ def test_adjoint_c2r_against_fd_and_torch(n):
     _fp64_ok(out, Xt.grad.numpy(), bound=1e-5, what="c2r adjoint vs torch")
 
 
-def test_twiddles_are_correctly_rounded_fp64_values():
-    """The GPU-generated FP32 twiddles equal the FP64 unit roots rounded to
-    FP32 (a 1-ulp allowance covers double-rounding ties)."""
-    with A.Plan.plan1d(4096, A.C2C, 1) as p:
+def _unit_root_fp32(m, M):
+    """exp(-2 pi i m / M) in FP64 rounded to complex64, with the angle reduced
+    exactly: 2m/M = q/2 + y with integer q and |y| <= 1/4 (y from an exact
+    integer numerator), so quarter-turn values come out exact (cos(pi/2) = 0,
+    not 6e-17)."""
+    m = np.asarray(m, dtype=np.int64) % M
+    q = (4 * m + M // 2) // M                      # nearest multiple of 1/2 of 2m/M
+    y = (4 * m - q * M).astype(np.float64) / (2.0 * M)
+    c, s = np.cos(np.pi * y), np.sin(np.pi * y)
+    q = q % 4
+    cr = np.select([q == 0, q == 1, q == 2, q == 3], [c, -s, -c, s])
+    sr = np.select([q == 0, q == 1, q == 2, q == 3], [s, c, -s, -c])
+    return (cr - 1j * sr).astype(np.complex64)
+
+
+@pytest.mark.parametrize("plan_args", [("1d", 4096, A.C2C, 1), ("1d", 3000, A.R2C, 4), ("1d", 1 << 20, A.C2C, 2),
+                                       ("1d", 46200, A.C2C, 1), ("2d", 2048, 1000, 1), ("1d", 1 << 25, A.R2C, 1)])
+def test_twiddles_are_correctly_rounded_fp64_values(plan_args):
+    """Every pass-table and linear-table entry of the GPU-generated blob
+    equals exp(-2 pi i m / M) for its documented index m, evaluated in FP64
+    and rounded to FP32: bit-exact except where FP64 rounding of the angle
+    lands next to an FP32 rounding tie (then within 1 ulp)."""
+    kind, a, bb, c = plan_args
+    p = A.Plan.plan1d(a, bb, c) if kind == "1d" else A.Plan.plan2d(c, a, bb, A.C2C)
+    with p:
         tw = p.twiddles()
-    assert tw.size > 0
-    mag = np.abs(tw.astype(np.complex128))
-    assert np.abs(mag - 1).max() < 2e-7
+        segs = p.twiddle_segments()
+    checked = exact_bits = 0
+    for off, cnt, M, param, k in segs:
+        if k not in (1, 2):
+            continue
+        i = np.arange(cnt, dtype=np.int64)
+        m = ((i // param) * (i % param)) % M if k == 2 else (i * param) % M
+        want = _unit_root_fp32(m, M)
+        got = tw[off: off + cnt]
+        gf, wf = got.view(np.float32), want.view(np.float32)
+        ulp = np.spacing(np.maximum(np.abs(wf), np.float32(1e-30)))
+        assert np.all(np.abs(gf - wf) <= ulp), (plan_args, off, M, param, k)
+        checked += gf.size
+        exact_bits += int(np.count_nonzero(gf == wf))
+    assert checked > 0
+    assert exact_bits >= 0.999 * checked, (exact_bits, checked)
 
 
 @pytest.mark.parametrize("kind,n,b", [("c2c", 4096, 64), ("c2c", 4096, 2048), ("c2c", 65536, 3), ("r2c", 3000, 37),

@@ -122,3 +122,13 @@ def test_stockham_index_maps_are_permutations(radices):
     rng = np.random.default_rng(L)
     x = rng.standard_normal(L) + 1j * rng.standard_normal(L)
     assert np.abs(O.stockham_simulate_exact(x, radices) - O.c2c(x[None])[0]).max() < 1e-10 * L
+
+
+def test_long_row_oracle_agrees_with_c_oracle():
+    """The numpy FP64 path used for the longest reference rows (2^23-2^27)
+    agrees with the C oracle to FP64 rounding at 2^20 and an odd length."""
+    rng = np.random.default_rng(11)
+    for n in (1 << 20, 999999):
+        x = rng.standard_normal((1, n))
+        a, b = O.r2c(x), O.r2c_long_rows(x)
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-13

@@ -6,7 +6,8 @@ synchronisation cudaMalloc/cudaFree may cause.  This entry point serves them:
 its intermediate lives in a fixed device array built into the library.  The
 test calls it through the C ABI twice in a row (different inputs, so stale
 scratch contents would show) and compares each result with the plan-based
-aclfftExecC2C on the same data.  It is collected last so that a run stopping
+aclfftExecC2C on the same data; an in-place case is checked directly
+against the FP64 oracle.  It is collected last so that a run stopping
 at the first failure has already run everything else, and it passes both on
 its own and after the rest of the suite.
 """
@@ -16,6 +17,7 @@ import numpy as np
 import pytest
 
 import aclfft as A
+import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -49,6 +51,26 @@ def test_no_alloc_matches_plan_path_on_two_calls(nx, batch):
             torch.cuda.synchronize()
             assert torch.isfinite(torch.view_as_real(out)).all()
             assert _rel(out, ref) <= REL_TOL, (call, _rel(out, ref))
+
+
+@pytest.mark.parametrize("nx,batch", [(65536, 4), (46200, 2)])
+def test_no_alloc_in_place_matches_fp64_oracle(nx, batch):
+    """idata == odata (documented as allowed: the intermediate lives in the
+    library's fixed array, never in the caller's buffer), checked directly
+    against the FP64 oracle on two calls in a row, forward then backward."""
+    dev = torch.device("cuda:0")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(nx)
+    for direction in (A.FORWARD, A.BACKWARD):
+        x = (rng.standard_normal((batch, nx)) + 1j * rng.standard_normal((batch, nx))).astype(np.complex64)
+        buf = torch.from_numpy(x).to(dev)
+        rc = A.lib().aclfftExecC2CNoAlloc(buf.data_ptr(), buf.data_ptr(), nx, batch, direction,
+                                         ctypes.c_void_p(stream.cuda_stream))
+        assert rc == A.SUCCESS, (rc, A.last_error_detail())
+        torch.cuda.synchronize()
+        e = O.errors(buf.cpu().numpy(), O.c2c(x, direction))
+        assert e["rel_l2"] <= 1e-5, (direction, e)
 
 
 def test_no_alloc_rejects_oversize_and_host_buffers():
