@@ -1,8 +1,8 @@
 #!/usr/bin/env python
 """Benchmark of the batched FP32 transform path on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5|long]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--reps R] [--impl ours|reference]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5|long] [--no-extras]
 
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
@@ -13,15 +13,21 @@ algorithmic bytes of the transforms only (one read of each transform's
 input + one write of its output) per second of the whole step.
 
 Timing: inputs resident in HBM, rotating buffer sets whose total exceeds
-2x the L2 size, W warm-up steps, then the K timed steps captured in one CUDA
-graph on the launch stream and replayed once between barriers and device
-synchronisation, timed with CUDA events on that stream, max over ranks.
-`roofline` times K launches of the dominant kernel (R2C, N=3000) over the
-same buffer sets the same way (one graph, one replay, CUDA events on the
-launch stream) and divides by K; `e2e` repeats the step through the C ABI with
-host (pinned) buffers, so the host<->device copies are inside the timing;
-`cpu_baseline` times the FP32 port of the reference's CPU-side algorithm
-(oracle port) on a bounded sample of the same workload.
+2x the L2 size, W warm-up steps, then the K steps captured in one CUDA graph
+on the launch stream, replayed R (>= 20) times, each replay between barriers
+and device synchronisation and timed with CUDA events on that stream;
+`value` comes from the median replay, max over ranks.  `roofline` times a
+graph of K launches of the dominant kernel (R2C, N=3000) over the same
+buffer sets the same way (median of R replays, divided by K); `e2e` repeats
+the step through the C ABI with host (pinned) buffers, so the host<->device
+copies are inside the timing; `cpu_baseline` times the reference's golden
+path (torch.fft on the host cores) on the same workload.
+
+With the default workload the line also carries, under `config`, the
+BASELINE cfg3 comparison of the split-precision tensor-core forms against
+the FP32 Stockham form with their FP64 errors, the per-length fractions of
+the HBM roofline at N = 4096-65536, and the same step run through the
+torch.autograd wrappers (loss.backward()).
 """
 from __future__ import annotations
 
@@ -595,7 +601,7 @@ class LongWorkload:
 
     def __init__(self, torch, A, dev, stream, nsets):
         self.torch, self.A = torch, A
-        g = torch.Generator(device="cpu").manual_seed(12345)
+        g = torch.Generator(device=dev).manual_seed(12345)  # drawn on the GPU: 1 GB per set
         self.items = []  # (kind, n, batch, plan, bytes)
         for n in self.LENGTHS:
             b = self.POINTS // n
@@ -609,10 +615,11 @@ class LongWorkload:
             s = {}
             for kind, n, b, _, _ in self.items:
                 if kind == "C2C":
-                    x = torch.complex(torch.randn((b, n), generator=g), torch.randn((b, n), generator=g)).to(dev)
+                    x = torch.complex(torch.randn((b, n), generator=g, device=dev),
+                                      torch.randn((b, n), generator=g, device=dev))
                     y = torch.empty_like(x)
                 else:
-                    x = torch.randn((b, n), generator=g).to(dev)
+                    x = torch.randn((b, n), generator=g, device=dev)
                     y = torch.empty((b, n // 2 + 1), dtype=torch.complex64, device=dev)
                 s[(kind, n)] = (x, y)
             self.sets.append(s)
@@ -720,48 +727,390 @@ def make_workload(name, torch, A, dev, stream, nsets):
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(wl, target_s=12.0):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+# The reference's own CPU implementation of this path is its golden path:
+# torch.fft on the host (pocketfft), called by its test-data generators,
+#   rfft            src/rfft1_d/tests/rfft1_d_data/gen_data.py:88
+#   irfft * n       src/irfft1_d/tests/irfft1_d_data/gen_data.py:62
+#   fft / ifft * n  src/fft1_d/tests/fft1_d_data/gen_data.py:71-86
+#   fft2 / ifft2    src/fft2_d/tests/fft2_d_data/gen_data.py:59-61
+# (its transform kernels are Ascend C and do not run on this host).  Each
+# golden step below runs the same transforms as the GPU step of the workload,
+# on seeded CPU inputs of the same shapes, and returns the algorithmic bytes.
+def golden_step(name, torch, fraction=1.0):
+    """(step closure, algorithmic bytes per step, description) of the
+    reference's golden path for workload `name` on `fraction` of its batch."""
+    g = torch.Generator().manual_seed(12345)
+    F = torch.fft
 
+    def rows(b):
+        return max(1, int(round(b * fraction)))
+
+    if name == "cfg2":
+        data = []
+        for n in (3000, 1024):
+            b = rows(4096)
+            nb = n // 2 + 1
+            half = torch.ones(nb)
+            half[1:(n + 1) // 2] = 0.5
+            data.append((n, torch.randn((b, n), generator=g), 2 * torch.rand((b, nb), generator=g), half))
+
+        def step():
+            for n, x, w2, half in data:
+                X = F.rfft(x, dim=1)
+                F.irfft(X, n=n, dim=1).mul_(n)
+                G = X * w2
+                F.irfft(G * half, n=n, dim=1).mul_(n)   # R2C adjoint: C2R of G, interior bins halved
+
+        byt = sum(3 * x.shape[0] * (n * 4 + (n // 2 + 1) * 8) for n, x, _, _ in data)
+        return step, byt, "per N in (3000, 1024): rfft, irfft*n, 2wX, irfft*n of the halved-interior gradient"
+    if name in ("cfg1", "cfg3"):
+        sizes = [(4096, 256)] if name == "cfg1" else [(65536, 64), (16384, 64)]
+        xs = [torch.complex(torch.randn((rows(b), n), generator=g), torch.randn((rows(b), n), generator=g))
+              for n, b in sizes]
+
+        def step():
+            for x in xs:
+                F.fft(x, dim=1)
+
+        return step, sum(16 * x.numel() for x in xs), "torch.fft.fft per length"
+    if name == "cfg4":
+        b = rows(8)
+        x = torch.complex(torch.rand((b, 2048, 2048), generator=g) * 2 - 1, torch.rand((b, 2048, 2048), generator=g) * 2 - 1)
+        G = torch.complex(torch.randn(x.shape, generator=g), torch.randn(x.shape, generator=g))
+
+        def step():
+            Y = F.fft2(x)
+            F.ifft2(Y)
+            F.ifft2(G).mul_(2048 * 2048)  # adjoint of the unnormalised forward
+
+        return step, 3 * 16 * x.numel(), "fft2, ifft2 (1/N^2), ifft2*N^2 of G"
+    if name == "cfg5":
+        import numpy as np
+
+        sys.path.insert(0, os.path.join(ROOT, "ops-fft_gb300"))
+        import aclfft as A  # only its seeded workload recipe (pure Python)
+
+        lengths, types = A.ragged_lengths(10000, seed=12345)
+        cnt = rows(len(lengths))
+        items = []
+        for n, t in zip(lengths[:cnt], types[:cnt]):
+            n = int(n)
+            if t == A.C2C:
+                items.append((True, torch.complex(torch.randn(n, generator=g), torch.randn(n, generator=g))))
+            else:
+                items.append((False, torch.randn(n, generator=g)))
+
+        def step():
+            for c2c, x in items:
+                F.fft(x) if c2c else F.rfft(x)
+
+        byt = int(sum(16 * x.numel() if c else 4 * x.numel() + 8 * (x.numel() // 2 + 1) for c, x in items))
+        return step, byt, f"{cnt} of the 10000 ragged transforms, one torch.fft call each"
+    if name == "long":
+        data = []
+        for n in (4096, 16384, 65536):
+            b = rows((1 << 25) // n)
+            data.append((torch.complex(torch.randn((b, n), generator=g), torch.randn((b, n), generator=g)),
+                         torch.randn((b, n), generator=g)))
+
+        def step():
+            for xc, xr in data:
+                F.fft(xc, dim=1)
+                F.rfft(xr, dim=1)
+
+        byt = sum(16 * xc.numel() + 4 * xr.numel() + 8 * xr.shape[0] * (xr.shape[1] // 2 + 1) for xc, xr in data)
+        return step, byt, "torch.fft.fft and rfft per length"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def time_golden(name, torch, threads, target_s, fraction=1.0, max_reps=50):
+    """GB/s of the golden path on `threads` host threads: one warm-up step,
+    then steps until about target_s seconds have passed."""
+    torch.set_num_threads(threads)
+    step, byt, what = golden_step(name, torch, fraction)
+    step()
+    reps, t = 0, 0.0
+    while reps < max_reps and (reps < 2 or t < target_s):
+        t0 = time.perf_counter()
+        step()
+        t += time.perf_counter() - t0
+        reps += 1
+    return byt * reps / t / 1e9, reps, what
+
+
+def cpu_baseline(wl, name, torch):
+    """The golden path on all host cores (the reported baseline), on one core,
+    and the FP32 port of the reference's arch35 algorithm (secondary)."""
     cores = os.cpu_count() or 1
-    rows = 64
-    done, dt = wl.cpu_sample(O, rows, cores)  # warm-up and size probe
-    reps = max(1, int(target_s / max(dt, 1e-3)))
-    rows_total = rows
-    if dt < target_s / 20:
-        rows_total = min(rows * int(target_s / 4 / max(dt, 1e-3)), 4096)
-        reps = 2
-    done = 0
-    t = 0.0
-    for _ in range(reps):
-        d, dt = wl.cpu_sample(O, rows_total, cores)
-        done += d
-        t += dt
-    return {"value": round(done / t / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-            "sample": f"{rows_total} rows per transform length x {reps} repetitions of the FP32 port of the "
-                      f"reference's R2C/C2R/C2C algorithm (oracle/oracle_fft.c port_*), OpenMP over rows"}
+    v_all, reps, what = time_golden(name, torch, cores, 6.0)
+    one_frac = 1.0 if name in ("cfg1", "cfg3", "cfg2") else 0.125
+    v_one, reps1, _ = time_golden(name, torch, 1, 4.0, fraction=one_frac, max_reps=10)
+    torch.set_num_threads(cores)
+    port = None
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        done, dt = wl.cpu_sample(O, 64, cores)
+        port = round(done / dt / 1e9, 3)
+    except Exception as e:  # noqa: BLE001 - the port is informational only
+        port = f"unavailable: {type(e).__name__}"
+    return {"value": round(v_all, 3), "unit": "GB/s", "cores": cores, "kind": "reference",
+            "sample": f"the reference's golden path, torch {torch.__version__} torch.fft on CPU ({what}), "
+                      f"full batch of the workload, {reps} steps on {cores} threads",
+            "single_thread_value": round(v_one, 3),
+            "single_thread_sample": f"{one_frac:g} of the batch, {reps1} steps on 1 thread",
+            "port_value": port,
+            "port_sample": "FP32 port of the reference's arch35 Stockham algorithm (oracle/oracle_fft.c port_*), "
+                           "64 rows per length"}
+
+
+# ------------------------------------------------------------------ timing
+class GraphTimer:
+    """Times fn(0..nk-1) as ONE CUDA graph on the work stream: captured,
+    replayed once untimed, then `reps` replays, each bracketed by a barrier
+    and device synchronisation and timed with CUDA events on that stream.
+    Returns the per-replay milliseconds (None if the capture fails)."""
+
+    def __init__(self, torch, stream, dist, notes):
+        self.torch, self.stream, self.dist, self.notes = torch, stream, dist, notes
+
+    def __call__(self, fn, nk, reps):
+        torch = self.torch
+        g = torch.cuda.CUDAGraph()
+        try:
+            with torch.cuda.graph(g, stream=self.stream):
+                for i in range(nk):
+                    fn(i)
+        except Exception as e:  # noqa: BLE001 - report and time eagerly instead
+            self.notes.append(f"graph capture failed ({type(e).__name__}: {str(e)[:120]}), eager launches")
+            torch.cuda.synchronize()
+            return None
+        g.replay()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(reps):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if self.dist:
+                self.dist.barrier()
+            torch.cuda.synchronize()
+            t0.record(self.stream)
+            g.replay()
+            t1.record(self.stream)
+            torch.cuda.synchronize()
+            out.append(t0.elapsed_time(t1))
+        if self.dist:
+            self.dist.barrier()
+        del g
+        return out
+
+    def eager(self, fn, nk, reps):
+        torch = self.torch
+        out = []
+        for _ in range(reps):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if self.dist:
+                self.dist.barrier()
+            torch.cuda.synchronize()
+            t0.record(self.stream)
+            for i in range(nk):
+                fn(i)
+            t1.record(self.stream)
+            torch.cuda.synchronize()
+            out.append(t0.elapsed_time(t1))
+        return out
+
+
+def spread(v):
+    return {"median": round(statistics.median(v), 5), "min": round(min(v), 5), "max": round(max(v), 5),
+            "reps": len(v)}
+
+
+def measure(wl, timer, nk, reps, warmup, torch):
+    """(median ms of nk steps, per-replay ms list, median ms per dominant
+    launch, per-item median ms for the long workload or None)."""
+    for i in range(warmup):
+        wl.step(i)
+    torch.cuda.synchronize()
+    steps = timer(wl.step, nk, reps) or timer.eager(wl.step, nk, reps)
+    dom = timer(wl.dom_call, nk, reps) or timer.eager(wl.dom_call, nk, reps)
+    per = None
+    if isinstance(wl, LongWorkload):
+        per = {}
+        for key in [(it[0], it[1]) for it in wl.items]:
+            f = lambda i, k=key: wl.item_call(k, i)
+            t = timer(f, nk, reps) or timer.eager(f, nk, reps)
+            per[key] = statistics.median(t) / nk
+    return statistics.median(steps), steps, statistics.median(dom) / nk, per
+
+
+def nsets_for(set_bytes, l2):
+    return max(1, -(-2 * l2 // max(set_bytes, 1)) + (1 if set_bytes < 4 * l2 else 0))
+
+
+def extra_split_tc_forms(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak):
+    """BASELINE cfg3 (C2C N = 65536 and 16384, batch 64) in every arithmetic
+    form: plain FP32 Stockham and the TF32x3 / BF16x3 split-precision
+    tensor-core forms, each with GB/s, its dominant launch and its rel-L2 /
+    max-abs error against torch's complex128 FFT of the same inputs."""
+    probe_bytes = 16 * (65536 * 64 + 16384 * 64)
+    wl = make_workload("cfg3", torch, A, dev, stream, nsets_for(probe_bytes, l2))
+    forms = {}
+    for prec in (A.PREC_FP32, A.PREC_TF32X3, A.PREC_BF16X3):
+        wl.set_prec(prec)
+        ms, _, dom, _ = measure(wl, timer, nk, reps, warmup, torch)
+        forms[wl.FORM_NAMES[prec]] = {
+            "GB/s": round(wl.alg_bytes_per_step * nk / (ms / 1e3) / 1e9, 1),
+            "frac_of_measured_hbm": round(wl.alg_bytes_per_step * nk / (ms / 1e3) / 1e9 / peak, 3),
+            "dominant_us": round(dom * 1e3, 2), "launches_per_step": wl.launches_per_step,
+            "fp64_error": wl.fp64_errors()}
+    del wl
+    torch.cuda.empty_cache()
+    fp32 = forms["fp32 stockham"]["GB/s"]
+    best_tc = max((k for k in forms if k != "fp32 stockham" and
+                   max(e["rel_l2"] for e in forms[k]["fp64_error"].values()) <= 1e-6),
+                  key=lambda k: forms[k]["GB/s"], default=None)
+    return {"workload": "C2C N=65536 and N=16384, batch 64, x ~ N(0,1) (BASELINE cfg3)", "forms": forms,
+            "fp64_reference": "torch.fft.fft in complex128 on the same device inputs",
+            "best_split_form_within_1e-6": best_tc,
+            "split_beats_fp32_within_1e-6": bool(best_tc and forms[best_tc]["GB/s"] > fp32)}
+
+
+def extra_long_lengths(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak):
+    """Batched C2C and R2C at N = 4096, 16384, 65536 with 2^25 complex points
+    per C2C launch (inputs far above L2): per-length launch time and fraction
+    of the measured HBM copy peak (the N = 4096-65536 >= 70 % target)."""
+    wl = make_workload("long", torch, A, dev, stream, 2)
+    _, _, _, per = measure(wl, timer, nk, reps, warmup, torch)
+    out = {}
+    for (kind, n), t_ms in per.items():
+        byt = next(it[4] for it in wl.items if (it[0], it[1]) == (kind, n))
+        gbs = byt / (t_ms / 1e3) / 1e9
+        out[f"{kind} {n}"] = {"batch": next(it[2] for it in wl.items if (it[0], it[1]) == (kind, n)),
+                              "us": round(t_ms * 1e3, 1), "GB/s": round(gbs, 1),
+                              "frac_of_measured_hbm": round(gbs / peak, 3)}
+    del wl
+    torch.cuda.empty_cache()
+    return out
+
+
+def extra_autograd(torch, dev, stream, nk, reps, warmup):
+    """The headline step through the torch.autograd wrappers (torch_fft):
+    X = rfft(x), y = irfft(X, n), loss = sum(w*|X|^2), loss.backward() -
+    the gradient runs the library's R2C adjoint kernel.  Timed as a CUDA
+    graph like the headline step; the gradient is compared with the explicit
+    adjoint call of the headline step."""
+    import torch_fft as TF
+
+    g = torch.Generator(device="cpu").manual_seed(12345)
+    b = 4096
+    data = []
+    for n in (3000, 1024):
+        x = torch.randn((b, n), generator=g).to(dev).requires_grad_(True)
+        w = torch.rand((b, n // 2 + 1), generator=g).to(dev)
+        data.append((n, x, w))
+
+    def step(i):
+        for n, x, w in data:
+            x.grad = None
+            X = TF.rfft(x)
+            TF.irfft(X.detach(), n)
+            loss = (w * (X.real ** 2 + X.imag ** 2)).sum()
+            loss.backward()
+
+    with torch.cuda.stream(stream):
+        for i in range(warmup):
+            step(i)
+    torch.cuda.synchronize()
+    # parity of the autograd gradient with the explicit adjoint (2wX -> R2C adjoint)
+    import aclfft as A
+
+    errs = {}
+    for n, x, w in data:
+        with torch.no_grad():
+            X = torch.fft.rfft(x.double())
+            ref = torch.fft.irfft(2 * w.double() * X * torch.cat(
+                [torch.ones(1, device=dev), torch.full(((n + 1) // 2 - 1,), 0.5, device=dev),
+                 torch.ones(n // 2 + 1 - (n + 1) // 2, device=dev)]).double(), n=n) * n
+            errs[str(n)] = float(torch.linalg.vector_norm(x.grad.double() - ref) / torch.linalg.vector_norm(ref))
+    gr = torch.cuda.CUDAGraph()
+    note = "one CUDA graph of the steps (forward + backward captured)"
+    try:
+        with torch.cuda.graph(gr, stream=stream):
+            for i in range(nk):
+                step(i)
+        gr.replay()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            t0.record(stream)
+            gr.replay()
+            t1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(t0.elapsed_time(t1))
+    except Exception as e:  # noqa: BLE001
+        note = f"eager (graph capture failed: {type(e).__name__})"
+        ts = []
+        for _ in range(reps):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            with torch.cuda.stream(stream):
+                t0.record(stream)
+                for i in range(nk):
+                    step(i)
+                t1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(t0.elapsed_time(t1))
+    ms = statistics.median(ts) / nk
+    byt = sum(3 * b * (n * 4 + (n // 2 + 1) * 8) for n in (3000, 1024))
+    TF.clear_cache()
+    return {"step": "per N in (3000, 1024): X = torch_fft.rfft(x), irfft(X), loss = sum(w|X|^2), loss.backward()",
+            "ms_per_step": round(ms, 4), "GB/s": round(byt / (ms / 1e3) / 1e9, 1), "timing": note,
+            "grad_rel_l2_vs_fp64_adjoint": errs}
 
 
 # ------------------------------------------------------------------- main
+def self_launch(gpus):
+    """`bench.py --gpus N` outside a launcher: run N ranks under
+    torch.distributed.run on this node (127.0.0.1) with the same arguments."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--reps", type=int, default=21, help="timed replays of the K-step graph (median reported)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg2")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="cfg2: skip the split-TC forms, per-length and autograd sub-measurements")
     ap.add_argument("--ragged-untuned", action="store_true",
                     help="cfg5: no autotuning and no graph replay (kernel profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    args.reps = max(args.reps, 20)
     Cfg5.untuned = args.ragged_untuned
 
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        return self_launch(args.gpus)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but the launcher started WORLD_SIZE={world} ranks")
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
@@ -782,84 +1131,15 @@ def main():
     torch.cuda.set_stream(stream)
     l2 = torch.cuda.get_device_properties(dev).L2_cache_size
     probe = make_workload(args.workload, torch, A, dev, stream, 1)
-    nsets = max(1, -(-2 * l2 // max(probe.set_bytes, 1)) + (1 if probe.set_bytes < 4 * l2 else 0))
+    nsets = nsets_for(probe.set_bytes, l2)
     del probe
     torch.cuda.empty_cache()
     wl = make_workload(args.workload, torch, A, dev, stream, nsets)
-    timing_mode = []
+    notes = []
+    timer = GraphTimer(torch, stream, dist, notes)
+    nk, reps = args.steps, args.reps
+    peak, peak_kind = _peaks()
 
-    def graph_ms(fn, nk):
-        """fn(0), ..., fn(nk-1) captured in ONE CUDA graph on the work stream,
-        replayed once untimed, then one replay timed with CUDA events on that
-        stream (barrier + synchronize on both sides).  None if capture fails."""
-        g = torch.cuda.CUDAGraph()
-        try:
-            with torch.cuda.graph(g, stream=stream):
-                for i in range(nk):
-                    fn(i)
-        except Exception as e:  # noqa: BLE001 - report and time eagerly instead
-            timing_mode.append(f"graph capture failed ({type(e).__name__}: {str(e)[:120]}), eager launches")
-            torch.cuda.synchronize()
-            return None
-        g.replay()
-        torch.cuda.synchronize()
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        t0.record(stream)
-        g.replay()
-        t1.record(stream)
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        del g
-        return t0.elapsed_time(t1)
-
-    def eager(nk):
-        if isinstance(wl, LongWorkload):
-            wl.reset_item_events()
-        dom_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nk)]
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        t0.record()
-        for i in range(nk):
-            wl.step(i, dom_ev[i])
-        t1.record()
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        if isinstance(wl, LongWorkload):
-            per = wl.item_times_ms()
-            return t0.elapsed_time(t1), per[wl.dom_key], per
-        return t0.elapsed_time(t1), statistics.mean(a.elapsed_time(b) for a, b in dom_ev), None
-
-    def timed(nk):
-        """(ms for nk steps, ms per dominant launch, per-item ms or None).
-        Steps: one graph of nk steps.  Dominant launch: one graph of nk
-        launches of that transform over the same rotating buffer sets."""
-        for i in range(args.warmup):
-            wl.step(i)
-        torch.cuda.synchronize()
-        ms = graph_ms(wl.step, nk)
-        if ms is None:
-            return eager(nk)
-        if isinstance(wl, LongWorkload):
-            per = {}
-            for key in [(it[0], it[1]) for it in wl.items]:
-                t = graph_ms(lambda i, k=key: wl.item_call(k, i), nk)
-                if t is None:
-                    return eager(nk)
-                per[key] = t / nk
-            return ms, per[wl.dom_key], per
-        t = graph_ms(wl.dom_call, nk)
-        if t is None:
-            return eager(nk)
-        return ms, t / nk, None
-
-    nk = args.steps
     forms = None
     if isinstance(wl, C2CWorkload):
         # every arithmetic form of the same workload, for comparison; the
@@ -868,7 +1148,7 @@ def main():
         own = wl.prec
         for prec in (A.PREC_FP32, A.PREC_BF16X3, A.PREC_TF32X3):
             wl.set_prec(prec)
-            f_ms, f_dom, _ = timed(nk)
+            f_ms, _, f_dom, _ = measure(wl, timer, nk, reps, args.warmup, torch)
             forms[wl.FORM_NAMES[prec]] = {
                 "GB/s": round(wl.alg_bytes_per_step * nk / (f_ms / 1e3) / 1e9, 1),
                 "dominant_us": round(f_dom * 1e3, 2), "launches_per_step": wl.launches_per_step,
@@ -877,19 +1157,19 @@ def main():
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     time.sleep(0.3)
-    ms, dom_ms, per_item = timed(nk)
+    ms, replays, dom_ms, per_item = measure(wl, timer, nk, reps, args.warmup, torch)
     clk = clocks.stop()
     ms = max_over_ranks(ms, dist, dev)
     ms_per_step = ms / nk
     value = whole_job_gbs(wl.alg_bytes_per_step, world, nk, ms / 1e3)
 
-    peak, peak_kind = _peaks()
     achieved = wl.dominant[1] / (dom_ms / 1e3) / 1e9
     traffic = NCU_TRAFFIC.get((args.workload, "dominant"))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
                 "kernel": wl.dominant[0], "alg_bytes_per_launch": wl.dominant[1],
-                "avg_launch_us": round(dom_ms * 1e3, 2)}
+                "avg_launch_us": round(dom_ms * 1e3, 2),
+                "timing": f"median of {reps} replays of a graph of {nk} launches, divided by {nk}"}
 
     e2e = None
     if not args.no_e2e:
@@ -908,19 +1188,32 @@ def main():
         te = max_over_ranks(te, dist, dev)
         e2e = {"value": round(whole_job_gbs(wl.alg_bytes_per_step, world, ke, te), 2), "unit": "GB/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "path": "aclfftExec* with pinned host buffers (library stages and synchronises)"}
+               "path": "aclfftExec* with pinned host buffers (library stages and synchronises)",
+               "steps_timed": ke}
+
+    extras = {}
+    if args.workload == "cfg2" and not args.no_extras:
+        del wl
+        torch.cuda.empty_cache()
+        extras["split_tc_vs_fp32"] = extra_split_tc_forms(torch, A, dev, stream, timer, nk, reps, args.warmup, l2,
+                                                          peak)
+        extras["per_length_n4096_65536"] = extra_long_lengths(torch, A, dev, stream, timer, nk, max(5, reps // 4),
+                                                              args.warmup, l2, peak)
+        extras["autograd_step"] = extra_autograd(torch, dev, stream, nk, max(5, reps // 4), args.warmup)
+        wl = make_workload(args.workload, torch, A, dev, stream, 1)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(wl)
+        cpu = cpu_baseline(wl, args.workload, torch)
 
     if rank == 0:
         cfg = wl.config()
         cfg["l2_strategy"] = f"{nsets} rotating buffer sets, {nsets * wl.set_bytes / 1e6:.0f} MB total > 2x L2 ({l2 / 1e6:.0f} MB)"
         cfg["parallelism"] = f"replicas x{world} (independent batches, no collective)"
-        cfg["timing"] = (timing_mode[-1] if timing_mode else
-                         f"one CUDA graph of {nk} steps (and one of {nk} dominant launches), one replay each timed "
-                         f"with CUDA events on the launch stream")
+        cfg["timing"] = (notes[-1] if notes else
+                         f"one CUDA graph of {nk} steps replayed {reps} times, each replay timed with CUDA events "
+                         f"on the launch stream between barriers; value from the median replay")
+        cfg["replay_ms"] = spread(replays)
         if isinstance(wl, (Cfg4, Cfg5)):
             cfg["fp64_error"] = wl.fp64_errors()
         if isinstance(wl, LongWorkload):
@@ -934,6 +1227,7 @@ def main():
         if forms is not None:
             cfg["forms"] = forms
             cfg["fp64_reference"] = "torch.fft.fft in complex128 on the same device inputs"
+        cfg.update(extras)
         line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": nk,
                 "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
@@ -945,60 +1239,40 @@ def main():
 
 
 def run_reference(args, rank, world):
-    """The reference's own implementation of the path on the host cores.
-
-    The reference ships no CPU transform: its kernels are Ascend C and its
-    golden path is torch.fft.  The arm therefore runs the FP32 port of the
-    reference's arch35 algorithm (oracle/oracle_fft.c port_*) with all host
-    threads, on a bounded sample of the same workload per step.
-    """
+    """The reference's own CPU implementation of the path: its golden
+    torch.fft path on the host cores (all threads), on the same workload and
+    full batch as our arm, K timed steps after W warm-up steps.  Under
+    torchrun only rank 0 runs and prints."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+    import torch
 
-    class _Shim:
-        pass
-
-    torch = None
-    wlname = args.workload
-    if wlname == "cfg2":
-        wl = Cfg2.__new__(Cfg2)
-        wl.sizes = (3000, 1024)
-        wl.batch = 4096
-        cfg = Cfg2.config(wl)
-        sample = lambda rows, th: Cfg2.cpu_sample(wl, O, rows, th)
-    elif wlname == "long":
-        wl = LongWorkload.__new__(LongWorkload)
-        wl.items = [(k, n, LongWorkload.POINTS // n, None, 0) for n in LongWorkload.LENGTHS for k in ("C2C", "R2C")]
-        cfg = LongWorkload.config(wl)
-        sample = lambda rows, th: LongWorkload.cpu_sample(wl, O, rows, th)
-    else:
-        wl = C2CWorkload.__new__(C2CWorkload)
-        wl.sizes = [(4096, 256)] if wlname == "cfg1" else [(65536, 64), (16384, 64)]
-        wl.name = wlname
-        cfg = C2CWorkload.config(wl)
-        sample = lambda rows, th: C2CWorkload.cpu_sample(wl, O, rows, th)
     cores = os.cpu_count() or 1
-    rows = 256
-    for _ in range(max(1, min(args.warmup, 2))):
-        sample(rows, cores)
-    done = 0
-    t = 0.0
+    torch.set_num_threads(cores)
+    fraction = 1.0 if args.workload in ("cfg1", "cfg2", "cfg3", "cfg4", "cfg5") else 0.125
+    step, byt, what = golden_step(args.workload, torch, fraction)
+    for _ in range(args.warmup):
+        step()
+    ts = []
     for _ in range(args.steps):
-        d, dt = sample(rows, cores)
-        done += d
-        t += dt
-    value = done / t / 1e9
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    t = sum(ts)
+    value = byt * args.steps / t / 1e9
+    cfg = {"workload": args.workload, "sample": f"{fraction:g} of the batch per step ({what})",
+           "same_config": fraction == 1.0}
+    sample = (f"the reference's golden path, torch {torch.__version__} torch.fft on CPU ({what}), {fraction:g} of "
+              f"the workload's batch per step, {cores} threads")
     line = {"metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
             "impl": "reference", "config": cfg,
-            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                             "sample": f"{rows} rows per transform length per step"},
+            "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "reference",
+                             "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main())

@@ -61,10 +61,7 @@ def test_max_over_ranks_and_whole_job_value_gloo():
 
 def test_reference_arm_under_torchrun_prints_once():
     # two ranks of the reference arm: rank 0 prints one JSON line, rank 1
-    # exits 0 without work (a tiny bounded sample, the FP32 port on the CPU)
-    oracle_lib = os.path.join(ROOT, "oracle", "_build")
-    if not os.path.isdir(oracle_lib):
-        pytest.skip("oracle not built")
+    # exits 0 without work (the golden torch.fft path on the CPU)
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2", "--master-addr",
            "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"), "--impl", "reference",
@@ -75,3 +72,19 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "reference" and d["config"]["same_config"]
+
+
+def test_gpus_flag_self_launches_ranks():
+    """`bench.py --gpus 2` outside a launcher starts two ranks itself; a
+    launcher whose WORLD_SIZE disagrees with --gpus is refused."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload", "cfg1", "--gpus", "2",
+           "--steps", "1", "--warmup", "1"]
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1 and json.loads(lines[0])["n_gpus"] == 2
+    env.update(WORLD_SIZE="1", RANK="0", LOCAL_RANK="0")
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
+    assert r.returncode != 0 and "WORLD_SIZE=1" in r.stderr
