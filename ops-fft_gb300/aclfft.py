@@ -163,6 +163,26 @@ _SIGNATURES = {
 }
 
 
+# include/aclfft_ops.h: the per-operator direct entries (aclError results)
+ACL_SUCCESS = 0
+ACL_ERROR_INVALID_PARAM = 100000
+ACL_ERROR_BAD_ALLOC = 200000
+ACL_ERROR_INTERNAL_ERROR = 500000
+_U = ctypes.c_uint32
+_OPS_STD = ["aclfftFft1DDft", "aclfftFft1DN", "aclfftFft1DB", "aclfftFft1DMix", "aclfftFft1DC2C", "aclfftFft1DC2CMix",
+            "aclfftRfft1DR2CFft", "aclfftRfft1DFft", "aclfftRfft1DDft", "aclfftIrfft1DFft", "aclfftIrfft1DDft",
+            "aclfftIrfft1DC2RFft"]
+_OPS_POW2 = ["aclfftRfft1DR2CFft1", "aclfftRfft1DR2CFft2", "aclfftRfft1DR2CFft31", "aclfftRfft1DR2CFft32",
+             "aclfftRfft1DR2CFft4", "aclfftRfft1DR2CFft5"]
+for _n in _OPS_STD:
+    _SIGNATURES[_n] = [_VP, _VP, _U, ctypes.c_int32, _U, _I, _VP]
+for _n in _OPS_POW2:
+    _SIGNATURES[_n] = [_VP, _VP, _U, _U, _I, _VP]
+_SIGNATURES["aclfftFft1DStride"] = [_VP, _VP, _U, ctypes.c_int32, _U, _U, _I, _VP]
+_SIGNATURES["aclfftRfft1D"] = [_VP, _VP, _U, ctypes.c_int32, _U, _VP]
+_SIGNATURES["aclfftFft2DDd"] = [_VP, _VP, _U, _U, _U, _I, _VP]
+
+
 def lib():
     """Load libops_fft.so (raises if it has not been built)."""
     global _lib

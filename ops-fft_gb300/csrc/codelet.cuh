@@ -242,8 +242,9 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
 }
 
 // Shared-memory layout (byte offsets from the dynamic shared base):
-//   [smem_tw, ...)                 pass tables (CTA-wide)
-//   [smem_post, ...)               post-process twiddles (CTA-wide)
+//   [0, 8)                         mbarrier of the table copies
+//   [smem_tw, ...)                 pass tables (CTA-wide), at smem_tw + (src % 16)
+//   [smem_post, ...)               post-process twiddles (CTA-wide), likewise
 //   [smem_stage + g*group_bytes)   group g: 64 B barriers/flags, then NST
 //                                  slots of stage_bytes.  A slot holds one
 //                                  transform: its raw input row at offset
@@ -262,8 +263,16 @@ template <class S, bool FC2R = false>
 __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_constant__ RowArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
-    float2* stw = reinterpret_cast<float2*>(smraw + A.smem_tw);
-    float2* spost = reinterpret_cast<float2*>(smraw + A.smem_post);
+    const float2* gtw = reinterpret_cast<const float2*>(A.tw);
+    const float2* gpost = reinterpret_cast<const float2*>(A.post_tw);
+    // tables: bulk copies of the 16-byte aligned supersets of the pass-table
+    // window and of the post-process twiddles; each lands at its region's
+    // start, so a table sits (src % 16) bytes in
+    const uintptr_t tw_src = reinterpret_cast<uintptr_t>(gtw + A.tw_lo);
+    const uintptr_t post_src = reinterpret_cast<uintptr_t>(gpost);
+    float2* stw = reinterpret_cast<float2*>(smraw + A.smem_tw + (tw_src & 15));
+    float2* spost = reinterpret_cast<float2*>(smraw + A.smem_post + (post_src & 15));
+    uint64_t* tbar = reinterpret_cast<uint64_t*>(smraw);
     constexpr int L = S::L;
     const int g = threadIdx.x / S::NTHR;
     const int tid = threadIdx.x - g * S::NTHR;
@@ -281,17 +290,6 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
     const int64_t gfirst = (int64_t)blockIdx.x * NG + g;
     const uintptr_t buf_lo = reinterpret_cast<uintptr_t>(A.in);
     const uintptr_t buf_hi = buf_lo + (uintptr_t)(A.ntf * row_bytes);
-    const float2* gtw = reinterpret_cast<const float2*>(A.tw);
-    const float2* gpost = reinterpret_cast<const float2*>(A.post_tw);
-
-    for (int i = threadIdx.x; i < A.tw_cnt; i += blockDim.x) stw[i] = ldg2(gtw + A.tw_lo + i);
-    for (int i = threadIdx.x; i < A.post_cnt; i += blockDim.x) spost[i] = ldg2(gpost + i);
-    if (leader) {
-        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
-        flags[0] = 0;
-        fence_mbar_init();
-    }
-    __syncthreads();  // the only CTA-wide barrier
 
     auto issue = [&](int s, int64_t t) {  // group leader only
         const uintptr_t src = buf_lo + (uintptr_t)(t * row_bytes);
@@ -306,12 +304,48 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             flags[1 + s] = 1;
         }
     };
+    // prologue: each group leader starts its input prefetches first (the
+    // longest latency), then thread 0 starts the table copies; no thread
+    // reads the tables before the table barrier completes
     uint32_t phase = 0;
     if (leader) {
+        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+        flags[0] = 0;
+        fence_mbar_init();
         for (int s = 0; s < NST; ++s) {
             const int64_t t = gfirst + (int64_t)s * gstride;
             if (t < A.ntf) issue(s, t);
         }
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t tw_bytes = A.tw_cnt > 0 ? (uint32_t)(((tw_src + (uintptr_t)A.tw_cnt * 8 + 15) & ~(uintptr_t)15) -
+                                                           (tw_src & ~(uintptr_t)15))
+                                               : 0u;
+        const uint32_t post_bytes =
+            A.post_cnt > 0 ? (uint32_t)(((post_src + (uintptr_t)A.post_cnt * 8 + 15) & ~(uintptr_t)15) -
+                                        (post_src & ~(uintptr_t)15))
+                           : 0u;
+        mbar_init(tbar, 1);
+        fence_mbar_init();
+        mbar_expect_tx(tbar, tw_bytes + post_bytes);
+        if (tw_bytes)
+            bulk_copy_g2s(smraw + A.smem_tw, reinterpret_cast<const void*>(tw_src & ~(uintptr_t)15), tw_bytes, tbar);
+        if (post_bytes)
+            bulk_copy_g2s(smraw + A.smem_post, reinterpret_cast<const void*>(post_src & ~(uintptr_t)15), post_bytes,
+                          tbar);
+    }
+    __syncthreads();  // the only CTA-wide barrier: barriers initialised
+    if (!mbar_wait_bounded(tbar, 0)) {
+        // the tables never arrived: record it and leave after the group's
+        // own copies have landed (or their wait ran out as well)
+        if (leader) {
+            atomicOr(A.err, 1);
+            for (int s = 0; s < NST; ++s) {
+                const int64_t t = gfirst + (int64_t)s * gstride;
+                if (t < A.ntf && !flags[1 + s]) mbar_wait_bounded(&bars[s], 0);
+            }
+        }
+        return;
     }
     const float2* tw = stw - A.tw_lo;
     const float2* post = spost;
@@ -426,31 +460,39 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             const float sc = A.scale;
             const float s2 = A.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
             constexpr int NPO = (L / 2 + 1 + S::NTHR - 1) / S::NTHR;  // pairs per thread
-            float2 za[NPO], zb[NPO], wk[NPO];
-            sfor<NPO>([&](auto qq) {
-                constexpr int q = decltype(qq)::value;
-                const int k = tid + q * S::NTHR;
-                if (k <= (L >> 1)) {
-                    za[q] = W[cpad<S>(k)];
-                    zb[q] = W[cpad<S>(L - k)];  // k = 0: entry L, unused
-                    wk[q] = post[k];
-                }
-            });
-            sfor<NPO>([&](auto qq) {
-                constexpr int q = decltype(qq)::value;
-                const int k = tid + q * S::NTHR;
-                if (k == 0) {
-                    const float2 z0 = za[q];
-                    c.out2[0] = make_float2((z0.x + z0.y) * sc, 0.f);
-                    c.out2[L] = make_float2((z0.x - z0.y) * sc, 0.f);
-                } else if (k <= (L >> 1)) {
-                    const float2 zk = za[q], zc = cconj(zb[q]);
-                    const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
-                    const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
-                    const float2 wo = cmul(wk[q], o);
-                    c.out2[k] = cscale(cadd(e, wo), s2);
-                    if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
-                }
+            // pairs are handled in chunks of PCH (all of them when few), every
+            // pair of a chunk read before any is stored; the reads only touch
+            // W and the stores only global memory, so chunks need no barrier
+            constexpr int PCH = NPO <= 8 ? NPO : 4;
+            sfor<(NPO + PCH - 1) / PCH>([&](auto cc) {
+                constexpr int q0 = decltype(cc)::value * PCH;
+                float2 za[PCH], zb[PCH], wk[PCH];
+                sfor<PCH>([&](auto qq) {
+                    constexpr int q = q0 + decltype(qq)::value;
+                    const int k = tid + q * S::NTHR;
+                    if (q < NPO && k <= (L >> 1)) {
+                        za[q - q0] = W[cpad<S>(k)];
+                        zb[q - q0] = W[cpad<S>(L - k)];  // k = 0: entry L, unused
+                        wk[q - q0] = post[k];
+                    }
+                });
+                sfor<PCH>([&](auto qq) {
+                    constexpr int q = q0 + decltype(qq)::value;
+                    const int k = tid + q * S::NTHR;
+                    if (q >= NPO) return;
+                    if (k == 0) {
+                        const float2 z0 = za[q - q0];
+                        c.out2[0] = make_float2((z0.x + z0.y) * sc, 0.f);
+                        c.out2[L] = make_float2((z0.x - z0.y) * sc, 0.f);
+                    } else if (k <= (L >> 1)) {
+                        const float2 zk = za[q - q0], zc = cconj(zb[q - q0]);
+                        const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+                        const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
+                        const float2 wo = cmul(wk[q - q0], o);
+                        c.out2[k] = cscale(cadd(e, wo), s2);
+                        if (L - k != k) c.out2[L - k] = cscale(cconj(csub(e, wo)), s2);
+                    }
+                });
             });
             group_sync<S>(bar_id);
         }

@@ -31,5 +31,8 @@
     X(14, 384, 2, 1500, 160, 15, 10, 10)       \
     X(15, 384, 2, 512, 64, 8, 8, 8)            \
     X(16, 384, 2, 256, 32, 16, 16)             \
-    X(17, 384, 2, 128, 32, 8, 16)
-#define GFFT_NUM_CODELETS 18
+    X(17, 384, 2, 128, 32, 8, 16)              \
+    X(18, 256, 1, 1500, 32, 15, 10, 10)        \
+    X(19, 256, 1, 1500, 32, 10, 10, 15)        \
+    X(20, 256, 1, 1500, 64, 15, 10, 10)
+#define GFFT_NUM_CODELETS 21

@@ -104,8 +104,11 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
         int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
         gfft_codelet_info(a.codelet, &cl, &cn, cr, &cnr, &cmaxt, &cminb);
         if (a.ngroups < 1 || a.ngroups > 15 || a.ngroups * a.ip.nthr > cmaxt) return fail(why, "codelet groups");
-        if (a.smem_tw < 128 || a.smem_post < a.smem_tw + (int64_t)a.tw_cnt * 8 ||
-            a.smem_stage < a.smem_post + (int64_t)a.post_cnt * 8 || a.smem_stage % 128 || a.group_bytes % 128 ||
+        // tables arrive as 16-byte aligned supersets: one spare unit each
+        const int64_t tw_need = a.tw_cnt > 0 ? (int64_t)a.tw_cnt * 8 + 16 : 0;
+        const int64_t post_need = a.post_cnt > 0 ? (int64_t)a.post_cnt * 8 + 16 : 0;
+        if (a.smem_tw < 128 || a.smem_tw % 16 || a.smem_post % 16 || a.smem_post < a.smem_tw + tw_need ||
+            a.smem_stage < a.smem_post + post_need || a.smem_stage % 128 || a.group_bytes % 128 ||
             a.stage_bytes % 16 || slots_end > a.group_bytes ||
             a.smem_bytes < a.smem_stage + (int64_t)a.ngroups * a.group_bytes || a.smem_bytes > kMaxSmemBytes)
             return fail(why, "codelet shared-memory layout");

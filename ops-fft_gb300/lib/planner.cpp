@@ -243,8 +243,11 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     if (even_mode) post_off = trial.add_linear(L / 2 + 1, 2 * (int64_t)L, 1);
     auto align = [](int64_t x, int64_t a) { return (x + a - 1) / a * a; };
     const int64_t hdr = 128;
-    const int64_t tw_bytes = align(tw_cnt * 8, 16);
-    const int64_t post_bytes = align(post_cnt * 8, 16);
+    // the tables arrive by bulk copies of their 16-byte aligned supersets
+    // (a table starting 8 bytes into a 16-byte unit sits 8 bytes in): one
+    // spare 16-byte unit each
+    const int64_t tw_bytes = tw_cnt > 0 ? align(tw_cnt * 8 + 16, 16) : 0;
+    const int64_t post_bytes = post_cnt > 0 ? align(post_cnt * 8 + 16, 16) : 0;
     const int tps = 1;
     // one transform per slot: raw row at offset src % 16 (< 16), padded work
     // layout from offset 16, both inside the slot

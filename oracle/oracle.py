@@ -43,8 +43,16 @@ def build(quiet: bool = True) -> str:
     return _LIB_PATH
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
+def reference_root() -> str:
+    """Where the reference tree is mounted: $OPS_FFT_REFERENCE, by default
+    /root/reference (only this container has it; nothing on a GPU machine
+    reads it)."""
+    return os.environ.get("OPS_FFT_REFERENCE", "/root/reference")
+
+
+def build_ref(ref_root: str | None = None) -> str | None:
     """Compile the reference's API layer into _ref/ when its sources exist."""
+    ref_root = ref_root or reference_root()
     if not os.path.isdir(os.path.join(ref_root, "lib")):
         return None
     out = subprocess.run(["make", "-C", _HERE, "ref", f"REF={ref_root}"], capture_output=True, text=True)

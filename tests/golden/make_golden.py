@@ -53,7 +53,7 @@ def _case_floats(op, cfg):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("OPS_FFT_REFERENCE", "/root/reference"))
     ap.add_argument("--max-floats", type=int, default=1 << 18)
     args = ap.parse_args()
     host = os.path.join(args.ref, "src", "common", "host")

@@ -21,19 +21,26 @@ def _declared(header):
 
 def test_library_loads_and_exports_every_declared_symbol():
     lib = A.lib()
-    names = _declared("cann_ops_fft.h") + _declared("aclfft_ext.h")
-    assert len(names) >= 25
+    names = _declared("cann_ops_fft.h") + _declared("aclfft_ext.h") + _declared("aclfft_ops.h")
+    assert len(names) >= 50
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
 
 def test_reference_header_surface_is_kept():
-    """Every function of the reference header is declared with the same name."""
-    ref = os.path.join("/root/reference", "include", "cann_ops_fft.h")
-    if not os.path.exists(ref):
+    """Every function of the reference's plan API header and of its
+    per-operator headers is declared here with the same name."""
+    root = O.reference_root()
+    if not os.path.exists(os.path.join(root, "include", "cann_ops_fft.h")):
         pytest.skip("reference tree not present")
-    ref_names = sorted(set(re.findall(r"ACLFFT_API\s+[\w\s\*]*?\b(aclfft\w+)\s*\(", open(ref).read())))
-    assert set(ref_names) <= set(_declared("cann_ops_fft.h"))
+    pat = r"ACLFFT_API\s+[\w\s\*]*?\b(aclfft\w+)\s*\("
+    ref = set(re.findall(pat, open(os.path.join(root, "include", "cann_ops_fft.h")).read()))
+    assert ref <= set(_declared("cann_ops_fft.h"))
+    ops = set()
+    for h in ("src/fft1_d/fft1_d.h", "src/rfft1_d/rfft1_d.h", "src/irfft1_d/irfft1_d.h", "src/fft2_d/fft2_d.h"):
+        ops |= set(re.findall(r"aclError\s+(aclfft\w+)\s*\(", open(os.path.join(root, h)).read()))
+    assert len(ops) >= 20
+    assert ops <= set(_declared("aclfft_ops.h")), ops - set(_declared("aclfft_ops.h"))
 
 
 def _ref_lib():
