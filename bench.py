@@ -7,10 +7,11 @@
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
 x ~ N(0,1) float32, loss = sum(w*|X|^2) with w ~ U[0,1].  One step runs,
-for each N: X = R2C(x), y = C2R(X), G = 2*w*X (the loss gradient, one torch
-elementwise kernel) and dx = R2C-adjoint(G).  `value` counts the
-algorithmic bytes of the transforms only (one read of each transform's
-input + one write of its output) per second of the whole step.
+for each N: X = R2C(x), y = C2R(X) and dx = dL/dx = R2C-adjoint(2*w*X), the
+weights 2w multiplied into X as the adjoint kernel loads it
+(aclfftExecR2CAdjointWeighted).  `value` counts the algorithmic bytes of
+the three transforms (one read of each transform's input + one write of its
+output; the weights' reads are not counted) per second of the whole step.
 
 Timing: inputs resident in HBM, rotating buffer sets whose total exceeds
 2x the L2 size, W warm-up steps, then the K steps captured in one CUDA graph
@@ -176,8 +177,7 @@ class Cfg2:
                 x = torch.randn((self.batch, n), generator=g).to(dev)
                 w2 = (2 * torch.rand((self.batch, nb), generator=g)).to(dev)
                 s[n] = dict(x=x, w2=w2, X=torch.empty((self.batch, nb), dtype=torch.complex64, device=dev),
-                            y=torch.empty_like(x), G=torch.empty((self.batch, nb), dtype=torch.complex64, device=dev),
-                            gx=torch.empty_like(x))
+                            y=torch.empty_like(x), gx=torch.empty_like(x))
             self.sets.append(s)
         self.bytes_per_transform = {n: self.batch * (n * 4 + (n // 2 + 1) * 8) for n in self.sizes}
         self.alg_bytes_per_step = sum(3 * b for b in self.bytes_per_transform.values())
@@ -202,8 +202,9 @@ class Cfg2:
                 else:
                     pr.exec_r2c(b["x"], b["X"])
                 pc.exec_c2r(b["X"], b["y"])
-                torch.mul(b["X"], b["w2"], out=b["G"])
-                pr.exec_r2c_adjoint(b["G"], b["gx"])
+                # dL/dx = R2C adjoint of 2wX: the weights are applied as the
+                # adjoint loads X (no separate elementwise pass)
+                pr.exec_r2c_adjoint_weighted(b["X"], b["w2"], b["gx"])
         self.stream.wait_stream(self.side)  # join: the step ends when both chains are done
 
     def dom_call(self, i):
@@ -220,7 +221,10 @@ class Cfg2:
             self.host[n] = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s.items()}
             for k, v in s.items():
                 self.host[n][k].copy_(v.cpu())
-            self.host[n]["G"].copy_(self.host[n]["X"] * 0 + 1)
+            # host buffers: the gradient 2wX is formed on the host and passed
+            # to the plain adjoint (the weighted entry takes device pointers)
+            self.host[n]["G"] = torch.empty(s["X"].shape, dtype=torch.complex64, pin_memory=True)
+            self.host[n]["G"].copy_((s["X"] * s["w2"]).cpu())
         h2d = sum(self.host[n][k].numel() * self.host[n][k].element_size()
                   for n in self.sizes for k in ("x", "X", "G"))
         d2h = sum(self.host[n][k].numel() * self.host[n][k].element_size()
@@ -274,8 +278,8 @@ class Cfg2:
     def config(self):
         return {"workload": "1D R2C->C2R round trip with gradients (loss sum(w*|X|^2))", "n": list(self.sizes),
                 "batch": self.batch, "dtype": "float32 / complex64 interleaved",
-                "step": "per N: R2C, C2R, G=2wX (torch), R2C adjoint; the N=1024 chain on a second stream "
-                        "forked from and joined to the launch stream"}
+                "step": "per N: X = R2C(x), y = C2R(X), dx = R2C adjoint of 2wX (weights applied as the adjoint "
+                        "loads X); the N=1024 chain on a second stream forked from and joined to the launch stream"}
 
 
 class C2CWorkload:

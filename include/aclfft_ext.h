@@ -71,6 +71,19 @@ ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* g
 ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftReal* gradIn);
 ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn);
 
+/* Weighted R2C adjoint (no counterpart in the reference): gradIn = the R2C
+ * adjoint of (weights * gradOut), weights real with the layout of the
+ * transform's output ([batch][nx/2+1] floats), multiplied in as the bins are
+ * loaded instead of by a separate elementwise pass.  For the loss
+ * sum(w*|X|^2) of X = R2C(x), gradOut = X and weights = 2w give dL/dx in one
+ * launch.  Device pointers only, out of place, asynchronous on the plan's
+ * stream; results are identical to scaling gradOut first and calling
+ * aclfftExecR2CAdjoint.  Available for even nx whose adjoint runs as one
+ * specialised row launch (aclfftGetPlanInfo: nsteps == 1, kernel >= 0, e.g.
+ * nx = 1024, 2048, 3000, 4096, 8192); ACLFFT_NOT_IMPLEMENTED otherwise. */
+ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const aclfftComplex* gradOut,
+                                                     const aclfftReal* weights, aclfftReal* gradIn);
+
 /* Plan introspection (for tests and tooling). */
 typedef struct aclfftPlanInfo_t {
     int supported;        /* 1 when the plan can execute on the GPU */

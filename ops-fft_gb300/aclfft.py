@@ -141,6 +141,7 @@ _SIGNATURES = {
     "aclfftExecC2CAdjoint": [_H, _VP, _VP, _I],
     "aclfftExecR2CAdjoint": [_H, _VP, _VP],
     "aclfftExecC2RAdjoint": [_H, _VP, _VP],
+    "aclfftExecR2CAdjointWeighted": [_H, _VP, _VP, _VP],
     "aclfftGetPlanInfo": [_H, ctypes.POINTER(PlanInfo)],
     "aclfftGetTwiddles": [_H, _VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
     "aclfftDebugCheckPlan": [_H, ctypes.c_char_p, _I],
@@ -278,6 +279,12 @@ class Plan:
 
     def exec_r2c_adjoint(self, g_out, g_in) -> None:
         _check(lib().aclfftExecR2CAdjoint(self.handle, ptr(g_out), ptr(g_in)), "aclfftExecR2CAdjoint")
+
+    def exec_r2c_adjoint_weighted(self, g_out, weights, g_in) -> None:
+        """g_in = R2C adjoint of (weights * g_out), the weights applied as the
+        bins are loaded (device tensors)."""
+        _check(lib().aclfftExecR2CAdjointWeighted(self.handle, ptr(g_out), ptr(weights), ptr(g_in)),
+               "aclfftExecR2CAdjointWeighted")
 
     def exec_c2r_adjoint(self, g_out, g_in) -> None:
         _check(lib().aclfftExecC2RAdjoint(self.handle, ptr(g_out), ptr(g_in)), "aclfftExecC2RAdjoint")

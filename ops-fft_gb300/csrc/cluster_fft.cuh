@@ -195,6 +195,25 @@ __global__ void __launch_bounds__(K::NT + 32, K::MINB) cluster_kernel(const __gr
     const uint32_t hdr = shared_u32(sm + K::O_HDR);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + K::O_HDR + 4);
 
+    // the first transform's column inputs are requested before anything
+    // else, so their HBM latency overlaps the table loads and the cluster
+    // barrier below (compute threads only; pf stays in registers)
+    const int ca = tid % PC, sa = tid / PC;  // column lane, butterfly slot
+    const float2* gin = static_cast<const float2*>(A.in);
+    float2 pf[NA0];
+    auto load_columns = [&](int64_t t) {
+        const float2* x = gin + t * A.in_dist + rank * PC + ca;
+        sfor<K::NBA0>([&](auto bb) {
+            constexpr int b = decltype(bb)::value;
+            const int j = sa + b * K::NSA;
+            sfor<K::Q0>([&](auto rr) {
+                constexpr int r = decltype(rr)::value;
+                pf[b * K::Q0 + r] = __ldcs(x + (int64_t)(j + r * (Q / K::Q0)) * P);
+            });
+        });
+    };
+    if (tid < K::NT && cid < A.ntf) load_columns(cid);
+
     for (int i = tid; i < Q; i += NTT) TQ[i] = __ldg(gtw + A.twq_off + i);
     for (int i = tid; i < P; i += NTT) TP[i] = __ldg(gtw + A.twp_off + i);
     for (int i = tid; i < (K::Q0 + K::Q1) * PC; i += NTT) {
@@ -259,26 +278,11 @@ __global__ void __launch_bounds__(K::NT + 32, K::MINB) cluster_kernel(const __gr
         }
     };
 
-    const int ca = tid % PC, sa = tid / PC;  // column lane, butterfly slot
     const int cb = tid % QC, sb = tid / QC;  // row lane, butterfly slot
     const uint32_t r_col = shared_u32(sm + K::O_R + rank * PC + ca);  // this lane's column, buffer 0
-    const float2* gin = static_cast<const float2*>(A.in);
     float2* gout = static_cast<float2*>(A.out);
     const float sc = A.scale;
     float2 v[K::E];
-    float2 pf[NA0];
-    auto load_columns = [&](int64_t t) {
-        const float2* x = gin + t * A.in_dist + rank * PC + ca;
-        sfor<K::NBA0>([&](auto bb) {
-            constexpr int b = decltype(bb)::value;
-            const int j = sa + b * K::NSA;
-            sfor<K::Q0>([&](auto rr) {
-                constexpr int r = decltype(rr)::value;
-                pf[b * K::Q0 + r] = __ldcs(x + (int64_t)(j + r * (Q / K::Q0)) * P);
-            });
-        });
-    };
-    if (cid < A.ntf) load_columns(cid);
     int64_t it = 0;
     for (int64_t t = cid; t < A.ntf; t += ncl, ++it) {
         const uint32_t b = (uint32_t)(it & 1);

@@ -142,8 +142,13 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
             //   Z'[0] = (x0 + xL, -(x0 - xL)) (imaginary parts of DC and Nyquist ignored)
             constexpr int L = S::L;
             const bool half = c.weight == WEIGHT_LOAD_HALF;
+            const float* wl = c.wl;
             load_all([&](int i) {
-                const float2 xi = c.st2[i], xm = c.st2[L - i];
+                float2 xi = c.st2[i], xm = c.st2[L - i];
+                if (wl) {
+                    xi = cscale(xi, __ldg(wl + i));
+                    xm = cscale(xm, __ldg(wl + (L - i)));
+                }
                 if (i == 0) return make_float2(xi.x + xm.x, -(xi.x - xm.x));
                 const bool lo = i <= (L >> 1);
                 float2 a = lo ? xi : xm, b = lo ? xm : xi;  // a = X[k], b = X[L-k]
@@ -403,6 +408,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         c.scale = A.scale;
         c.out2 = reinterpret_cast<float2*>(A.out) + t * A.out_dist;
         c.out1 = reinterpret_cast<float*>(A.out) + t * A.out_dist;
+        c.wl = A.wload ? A.wload + t * A.wdist : nullptr;
 
         bool from_slot = true;
         if (!FC2R && A.io_mode == IO_C2R_EVEN) {
@@ -418,6 +424,10 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                 if (k <= (L >> 1)) {
                     pa[q] = c.st2[k];
                     pb[q] = c.st2[L - k];
+                    if (c.wl) {
+                        pa[q] = cscale(pa[q], __ldg(c.wl + k));
+                        pb[q] = cscale(pb[q], __ldg(c.wl + (L - k)));
+                    }
                 }
             });
             group_sync<S>(bar_id);
@@ -543,6 +553,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) coltile_kernel(const __grid_
     c.conj_in = 0;
     c.conj_out = 0;
     c.scale = 1.f;
+    c.wl = nullptr;
     float2 v[S::E];
     float2* W = tile + (int64_t)g * A.wsize;
 

@@ -80,6 +80,10 @@ struct RowArgs {
     int32_t codelet;   // compile-time specialised kernel id, -1 for the generic kernel
     int32_t ngroups;   // codelets: transform groups per CTA
     int32_t group_bytes;  // codelets: shared bytes per group (barriers, slots, work buffer)
+    // codelets, even C2R: optional real weights multiplied into the input
+    // bins as they are loaded (bin k of transform t times wload[t*wdist + k])
+    const float* wload;
+    int64_t wdist;
 };
 
 // Strided ("column") transforms, optionally one outer Stockham pass of a

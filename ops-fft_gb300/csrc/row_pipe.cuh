@@ -37,6 +37,7 @@ struct PipeCtx {
     float* out1;
     int mode, conj_in, conj_out, weight, nreal;
     float scale;
+    const float* wl;  // codelets, even C2R: per-bin input weights of this transform (or nullptr)
 
     __device__ __forceinline__ int pad(int i) const { return i + (i >> pshift); }
     __device__ __forceinline__ float2* buf(int b) const { return b == 1 ? sA : sB; }
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(kernel_max_threads<RMAX>()) row_kernel(const _
         }
 
         PipeCtx c;
+        c.wl = nullptr;
         c.L = L;
         c.nthr = nthr;
         c.tid = tid;

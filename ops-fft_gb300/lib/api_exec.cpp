@@ -88,7 +88,7 @@ float norm_scale(const aclfftHandle_t* h, bool backward_like)
 }
 
 int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStream_t st, bool c2c, bool inverse,
-                float scale)
+                float scale, const float* wload = nullptr)
 {
     void* bufs[4] = {in, out, impl->ws, impl->ws2};
     const float2* tw = static_cast<const float2*>(impl->tw);
@@ -111,6 +111,10 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
                 s.row.conj_out = last && inverse;
             }
             if (last) s.row.scale = scale;
+            if (first && wload) {
+                s.row.wload = wload;
+                s.row.wdist = s.row.in_dist;
+            }
             rc = gfft_launch_row(&s.row, st);
             break;
         case Step::COL:
@@ -436,6 +440,49 @@ ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* g
     if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 2, gradOut, gradIn, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false,
                        false);
+}
+
+ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const aclfftComplex* gradOut,
+                                                     const aclfftReal* weights, aclfftReal* gradIn)
+{
+    EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_R2C);
+    ACLFFT_CHECK_NULL(weights);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    PlanImpl* impl = plan->impl;
+    if (!impl) return ACLFFT_INTERNAL_ERROR;
+    const StepList& sl = impl->lists[2];
+    // the weights ride on the even-C2R pre-process of a single codelet launch
+    if (!sl.supported || sl.steps.size() != 1 || sl.steps[0].kind != Step::ROW || sl.steps[0].row.codelet < 0 ||
+        sl.steps[0].row.io_mode != gfft::IO_C2R_EVEN) {
+        gfft::set_last_error("weighted adjoint: this length's adjoint is not one codelet launch");
+        return ACLFFT_NOT_IMPLEMENTED;
+    }
+    if (static_cast<const void*>(gradOut) == static_cast<const void*>(gradIn)) {
+        gfft::set_last_error("weighted adjoint: in-place calls are not supported");
+        return ACLFFT_INVALID_VALUE;
+    }
+    if (!impl->device_ready) {
+        if (gfft::plan_device_setup(impl) != ACLFFT_SUCCESS || !impl->device_ready) {
+            gfft::set_last_error("no usable CUDA device");
+            return ACLFFT_EXEC_FAILED;
+        }
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return ACLFFT_EXEC_FAILED;
+    }
+    if (dev != impl->device) return ACLFFT_INVALID_DEVICE;
+    if (classify(gradOut, dev) != Mem::DEVICE || classify(gradIn, dev) != Mem::DEVICE ||
+        classify(weights, dev) != Mem::DEVICE) {
+        gfft::set_last_error("weighted adjoint: device pointers of the plan's device only");
+        return ACLFFT_INVALID_VALUE;
+    }
+    const float scale = norm_scale(plan, false);
+    return launch_list(impl, sl, const_cast<aclfftComplex*>(gradOut), gradIn, plan->stream, false, false, scale,
+                       weights) == 0
+               ? ACLFFT_SUCCESS
+               : ACLFFT_EXEC_FAILED;
 }
 
 ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn)

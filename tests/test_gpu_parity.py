@@ -568,6 +568,52 @@ def _unit_root_fp32(m, M):
     return (cr - 1j * sr).astype(np.complex64)
 
 
+@pytest.mark.parametrize("n,b", [(3000, 64), (1024, 37), (2048, 5), (8192, 3)])
+def test_weighted_r2c_adjoint(n, b):
+    """aclfftExecR2CAdjointWeighted(X, 2w) = dL/dx of L = sum(w*|X|^2),
+    X = R2C(x): bit-identical to scaling X by 2w first and calling the plain
+    adjoint, and equal to the FP64 gradient (torch autograd in complex128)."""
+    dev = _dev()
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((b, n))
+    w = rng.uniform(0, 1, (b, n // 2 + 1))
+    xd = torch.tensor(x, dtype=torch.float32, device=dev)
+    w2 = torch.tensor(2 * w, dtype=torch.float32, device=dev)
+    X = torch.empty((b, n // 2 + 1), dtype=torch.complex64, device=dev)
+    g1 = torch.empty((b, n), dtype=torch.float32, device=dev)
+    g2 = torch.empty_like(g1)
+    with A.Plan.plan1d(n, A.R2C, b) as p:
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_r2c(xd, X)
+        p.exec_r2c_adjoint_weighted(X, w2, g1)
+        G = X * w2
+        p.exec_r2c_adjoint(G, g2)
+        torch.cuda.synchronize()
+        assert p.exec_error() == 0
+    assert torch.equal(g1, g2)
+    xt = torch.tensor(xd.cpu().numpy(), dtype=torch.float64, requires_grad=True)
+    (torch.tensor(w2.cpu().numpy(), dtype=torch.float64) / 2 * torch.fft.rfft(xt).abs() ** 2).sum().backward()
+    _fp64_ok(g1.cpu().numpy(), xt.grad.numpy(), what=("weighted adjoint", n))
+
+
+def test_weighted_r2c_adjoint_domain():
+    dev = _dev()
+    for n, b in ((65536, 2), (999, 3), (1 << 20, 1)):
+        X = torch.zeros((b, n // 2 + 1), dtype=torch.complex64, device=dev)
+        w = torch.ones((b, n // 2 + 1), dtype=torch.float32, device=dev)
+        g = torch.empty((b, n), dtype=torch.float32, device=dev)
+        with A.Plan.plan1d(n, A.R2C, b) as p:
+            rc = A.lib().aclfftExecR2CAdjointWeighted(p.handle, X.data_ptr(), w.data_ptr(), g.data_ptr())
+            assert rc == A.NOT_IMPLEMENTED, (n, rc)
+    with A.Plan.plan1d(3000, A.R2C, 2) as p:
+        X = torch.zeros((2, 1501), dtype=torch.complex64, device=dev)
+        hw = np.ones((2, 1501), dtype=np.float32)
+        g = torch.empty((2, 3000), dtype=torch.float32, device=dev)
+        assert A.lib().aclfftExecR2CAdjointWeighted(p.handle, X.data_ptr(), hw.ctypes.data, g.data_ptr()) == \
+            A.INVALID_VALUE
+        assert A.lib().aclfftExecR2CAdjointWeighted(p.handle, X.data_ptr(), None, g.data_ptr()) == A.INVALID_VALUE
+
+
 @pytest.mark.parametrize("plan_args", [("1d", 4096, A.C2C, 1), ("1d", 3000, A.R2C, 4), ("1d", 1 << 20, A.C2C, 2),
                                        ("1d", 46200, A.C2C, 1), ("2d", 2048, 1000, 1), ("1d", 1 << 25, A.R2C, 1)])
 def test_twiddles_are_correctly_rounded_fp64_values(plan_args):
