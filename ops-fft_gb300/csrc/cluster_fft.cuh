@@ -49,6 +49,7 @@
 #include "butterfly.cuh"
 #include "cluster_list.h"
 #include "kernel_args.h"
+#include "pdl.cuh"
 
 namespace gfft {
 namespace {
@@ -195,9 +196,9 @@ __global__ void __launch_bounds__(K::NT + 32, K::MINB) cluster_kernel(const __gr
     const uint32_t hdr = shared_u32(sm + K::O_HDR);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(sm + K::O_HDR + 4);
 
-    // the first transform's column inputs are requested before anything
-    // else, so their HBM latency overlaps the table loads and the cluster
-    // barrier below (compute threads only; pf stays in registers)
+    // the first transform's column inputs are requested right after the
+    // table loads, before the barrier set-up (compute threads only; pf
+    // stays in registers)
     const int ca = tid % PC, sa = tid / PC;  // column lane, butterfly slot
     const float2* gin = static_cast<const float2*>(A.in);
     float2 pf[NA0];
@@ -212,8 +213,6 @@ __global__ void __launch_bounds__(K::NT + 32, K::MINB) cluster_kernel(const __gr
             });
         });
     };
-    if (tid < K::NT && cid < A.ntf) load_columns(cid);
-
     for (int i = tid; i < Q; i += NTT) TQ[i] = __ldg(gtw + A.twq_off + i);
     for (int i = tid; i < P; i += NTT) TP[i] = __ldg(gtw + A.twp_off + i);
     for (int i = tid; i < (K::Q0 + K::Q1) * PC; i += NTT) {
@@ -229,6 +228,11 @@ __global__ void __launch_bounds__(K::NT + 32, K::MINB) cluster_kernel(const __gr
         for (int i = tid; i < P; i += NTT) TX[i] = __ldg(gpost + (int64_t)i * Q);  // W_{2N}^{Q*k_p}
         for (int i = tid; i <= H; i += NTT) TX[P + i] = __ldg(gpost + (i < H ? (int)rank * H + i : Q / 2));
     }
+    // the tables above belong to the plan; everything below touches the
+    // caller's buffers, so it waits for the grids this launch depends on
+    // (the first column loads then overlap the barrier set-up)
+    pdl_wait();
+    if (tid < K::NT && cid < A.ntf) load_columns(cid);
     if (tid == 0) {
         mb_init(hdr + 0, 1 + K::NT);
         mb_init(hdr + 8, 1 + K::NT);
@@ -572,14 +576,9 @@ int launch_t(const ClusterArgs* a, cudaStream_t st)
     attr[0].val.clusterDim.x = K::C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3((unsigned)(ncl * K::C), 1, 1);
-    cfg.blockDim = dim3(K::NT + 32, 1, 1);
-    cfg.dynamicSmemBytes = K::SMEM;
-    cfg.stream = st;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, cluster_kernel<K, MODE>, *a);
-    return (int)e;
+    (void)cfg;
+    return (int)launch_pdl(cluster_kernel<K, MODE>, dim3((unsigned)(ncl * K::C)), dim3(K::NT + 32), (size_t)K::SMEM,
+                           st, *a, &attr[0]);
 }
 
 #define GFFT_CL_SPEC(ID, N, C, Q, P, NT, MB, Q0, Q1, P0, P1) ClSpec<ID, N, C, Q, P, NT, MB, Q0, Q1, P0, P1>

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pdl.cuh"
 #include "row_pipe.cuh"
 
 namespace gfft {
@@ -309,19 +310,11 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             flags[1 + s] = 1;
         }
     };
-    // prologue: each group leader starts its input prefetches first (the
-    // longest latency), then thread 0 starts the table copies; no thread
-    // reads the tables before the table barrier completes
+    // prologue: thread 0 starts the table copies (plan-owned memory, safe
+    // before the wait for the preceding grid), then each group leader starts
+    // its input prefetches once that grid is complete; no thread reads the
+    // tables before the table barrier completes
     uint32_t phase = 0;
-    if (leader) {
-        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
-        flags[0] = 0;
-        fence_mbar_init();
-        for (int s = 0; s < NST; ++s) {
-            const int64_t t = gfirst + (int64_t)s * gstride;
-            if (t < A.ntf) issue(s, t);
-        }
-    }
     if (threadIdx.x == 0) {
         const uint32_t tw_bytes = A.tw_cnt > 0 ? (uint32_t)(((tw_src + (uintptr_t)A.tw_cnt * 8 + 15) & ~(uintptr_t)15) -
                                                            (tw_src & ~(uintptr_t)15))
@@ -338,6 +331,16 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         if (post_bytes)
             bulk_copy_g2s(smraw + A.smem_post, reinterpret_cast<const void*>(post_src & ~(uintptr_t)15), post_bytes,
                           tbar);
+    }
+    pdl_wait();
+    if (leader) {
+        for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
+        flags[0] = 0;
+        fence_mbar_init();
+        for (int s = 0; s < NST; ++s) {
+            const int64_t t = gfirst + (int64_t)s * gstride;
+            if (t < A.ntf) issue(s, t);
+        }
     }
     __syncthreads();  // the only CTA-wide barrier: barriers initialised
     if (!mbar_wait_bounded(tbar, 0)) {
@@ -529,6 +532,7 @@ template <class S>
 __global__ void __launch_bounds__(S::MAXT, S::MINB) coltile_kernel(const __grid_constant__ ColArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
+    pdl_wait();
     constexpr int L = S::L;
     const int TF = A.tfpc;
     const int g = threadIdx.x / S::NTHR;

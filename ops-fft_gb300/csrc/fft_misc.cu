@@ -32,6 +32,7 @@ __global__ void twiddle_kernel(float2* __restrict__ out, TwSeg seg)
 // CTA (see the fused versions in stockham.cuh for the formulas).
 __global__ void pack_kernel(PackArgs a)
 {
+    pdl_wait();
     const int L = a.L;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k > (L >> 1)) return;
@@ -125,8 +126,7 @@ extern "C" int gfft_launch_pack(const PackArgs* a, void* stream)
     if (a->ntf <= 0 || a->L < 1) return (int)cudaErrorInvalidValue;
     const int n = (a->L >> 1) + 1;
     dim3 grid((n + 255) / 256, (unsigned)(a->ntf < 65535 ? a->ntf : 65535));
-    pack_kernel<<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(*a);
-    return (int)cudaGetLastError();
+    return (int)launch_pdl(pack_kernel, grid, dim3(256), 0, static_cast<cudaStream_t>(stream), *a);
 }
 
 extern "C" int gfft_gen_twiddles(void* table, const TwSeg* segs, int nseg, void* stream)

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include "codelet.cuh"
+#include "pdl.cuh"
 #include "codelet_list.h"
 #include "row_pipe.cuh"
 #include "stockham.cuh"
@@ -58,8 +59,7 @@ int launch_row_t(const RowArgs* a, cudaStream_t st)
     if (a->grid > 0) grid = a->grid;
     if (grid < 1) grid = 1;
     if (grid > ntiles) grid = ntiles;
-    row_kernel<RMAX><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
-    return (int)cudaGetLastError();
+    return (int)launch_pdl(row_kernel<RMAX>, dim3((unsigned)grid), dim3(threads), (size_t)a->smem_bytes, st, *a);
 }
 
 template <int RMAX>
@@ -74,8 +74,7 @@ int launch_col_t(const ColArgs* a, cudaStream_t st)
     if (e != cudaSuccess) return (int)e;
     const int64_t grid = (a->ncols + a->tfpc - 1) / a->tfpc;
     if (grid > 0x7fffffff) return (int)cudaErrorInvalidValue;
-    col_kernel<RMAX><<<(unsigned)grid, threads, smem, st>>>(*a);
-    return (int)cudaGetLastError();
+    return (int)launch_pdl(col_kernel<RMAX>, dim3((unsigned)grid), dim3(threads), smem, st, *a);
 }
 
 template <class S, bool FC2R = false>
@@ -104,8 +103,7 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
     if (a->grid > 0) grid = a->grid;
     if (grid < 1) grid = 1;
     if (grid > ctas_needed) grid = ctas_needed;
-    codelet_kernel<S, FC2R><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
-    return (int)cudaGetLastError();
+    return (int)launch_pdl(codelet_kernel<S, FC2R>, dim3((unsigned)grid), dim3(threads), (size_t)a->smem_bytes, st, *a);
 }
 
 template <class S>
@@ -131,8 +129,7 @@ int launch_coltile_t(const ColArgs* a, cudaStream_t st)
     int64_t grid = (int64_t)sm_count() * last_occ;
     if (grid < 1) grid = 1;
     if (grid > ntiles) grid = ntiles;
-    coltile_kernel<S><<<(unsigned)grid, threads, (size_t)a->smem_bytes, st>>>(*a);
-    return (int)cudaGetLastError();
+    return (int)launch_pdl(coltile_kernel<S>, dim3((unsigned)grid), dim3(threads), (size_t)a->smem_bytes, st, *a);
 }
 
 #define GFFT_DECL_LAUNCH(ID, ...)                           \

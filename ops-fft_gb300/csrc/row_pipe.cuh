@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "pipe_ptx.cuh"
+#include "pdl.cuh"
 #include "stockham.cuh"
 
 namespace gfft {
@@ -113,6 +114,7 @@ __device__ __forceinline__ void coop_copy(void* dst, const void* src, int64_t by
 template <int RMAX>
 __global__ void __launch_bounds__(kernel_max_threads<RMAX>()) row_kernel(const __grid_constant__ RowArgs A)
 {
+    pdl_wait();  // every access below may touch the caller's buffers
     extern __shared__ __align__(128) unsigned char smraw[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smraw);   // up to 4 stages
     volatile int* flags = reinterpret_cast<int*>(smraw + 64);  // [0] abort, [1+s] manual copy of stage s

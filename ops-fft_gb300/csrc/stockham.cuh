@@ -35,6 +35,7 @@
 
 #include "butterfly.cuh"
 #include "kernel_args.h"
+#include "pdl.cuh"
 
 namespace gfft {
 
@@ -283,6 +284,7 @@ __device__ __forceinline__ void col_body(const ColArgs& A)
 template <int RMAX>
 __global__ void __launch_bounds__(kernel_max_threads<RMAX>()) col_kernel(const __grid_constant__ ColArgs A)
 {
+    pdl_wait();  // every access below may touch the caller's buffers
     col_body<RMAX>(A);
 }
 
