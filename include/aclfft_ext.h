@@ -104,9 +104,28 @@ typedef struct aclfftPlanInfo_t {
     int tc_stages;             /* tensor-core DFT-matrix launches per exec (0: FP32 kernels only) */
     int cluster_ctas;          /* CTAs per thread-block cluster of a cluster transform (0: none) */
     int cluster_count;         /* clusters resident at once on the plan's device (0: not prepared) */
+    int tuned;                 /* 1 when the launches were chosen by the autotuner (timed or cached) */
+    int tune_candidates;       /* distinct candidates the last tuning timed (0: taken from the cache) */
 } aclfftPlanInfo;
 
 ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* info);
+
+/* Autotuning (no counterpart in the reference, whose radix choices are
+ * fixed tables).  mode 1 times the planner's candidate choices for this
+ * plan - every specialised row-kernel build of its length, their transform
+ * groups per CTA and prefetch stages, the thread-block-cluster sizes and
+ * cluster-or-row-kernel for 4096-point transforms, no specialised kernels -
+ * on scratch buffers of the plan's shape (batch capped at 256 MB of input)
+ * and re-plans with the fastest; the planner's own choice is kept unless
+ * another is at least 2 % faster.  Called on a made plan it tunes at once,
+ * before MakePlan it makes MakePlan tune (OPS_FFT_AUTOTUNE=1 does this for
+ * every plan).  Needs a device; allocates scratch for the duration, so call
+ * it outside stream capture.  Choices are cached per (device, type, lengths,
+ * batch, layout) for the process and in the file named by
+ * OPS_FFT_PLAN_TUNE_CACHE (a damaged line is ignored).  Split-precision
+ * and VERTICAL plans have nothing to tune.  mode 0 (default) plans by the
+ * static rules. */
+ACLFFT_API aclfftResult aclfftSetAutotune(aclfftHandle plan, int mode);
 
 /* Copies the plan's FP32 twiddle blob (as generated on the GPU) to host
  * memory: at most maxEntries complex values; *entries receives the total. */

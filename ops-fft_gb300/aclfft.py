@@ -76,6 +76,8 @@ class PlanInfo(ctypes.Structure):
         ("tc_stages", ctypes.c_int),
         ("cluster_ctas", ctypes.c_int),
         ("cluster_count", ctypes.c_int),
+        ("tuned", ctypes.c_int),
+        ("tune_candidates", ctypes.c_int),
     ]
 
 
@@ -143,6 +145,7 @@ _SIGNATURES = {
     "aclfftExecC2RAdjoint": [_H, _VP, _VP],
     "aclfftExecR2CAdjointWeighted": [_H, _VP, _VP, _VP],
     "aclfftGetPlanInfo": [_H, ctypes.POINTER(PlanInfo)],
+    "aclfftSetAutotune": [_H, _I],
     "aclfftGetTwiddles": [_H, _VP, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
     "aclfftDebugCheckPlan": [_H, ctypes.c_char_p, _I],
     "aclfftExecC2CNoAlloc": [_VP, _VP, _I, _I, _I, _VP],
@@ -259,6 +262,10 @@ class Plan:
     def set_precision(self, mode: int) -> None:
         """PREC_FP32 (Stockham), PREC_TF32X3 or PREC_BF16X3 (tensor-core DFT stages)."""
         _check(lib().aclfftSetPrecisionMode(self.handle, mode), "aclfftSetPrecisionMode")
+
+    def set_autotune(self, on: bool = True) -> None:
+        """Time the planner's candidate choices for this plan and keep the fastest."""
+        _check(lib().aclfftSetAutotune(self.handle, int(bool(on))), "aclfftSetAutotune")
 
     def precision(self) -> int:
         m = _I()

@@ -20,6 +20,7 @@
 
 #include "handle.h"
 
+using gfft::Kind;
 using gfft::PlanImpl;
 using gfft::Step;
 using gfft::StepList;
@@ -394,6 +395,13 @@ size_t half_elems(const aclfftHandle_t* h) { return (size_t)h->batch * (size_t)(
 
 namespace gfft {
 void set_last_error(const std::string& s) { g_last_error = s; }
+
+int launch_primary(PlanImpl* impl, void* in, void* out, cudaStream_t st)
+{
+    const StepList& sl = impl->lists[0];
+    if (!sl.supported || missing_workspace(impl, sl)) return (int)cudaErrorInvalidValue;
+    return launch_list(impl, sl, in, out, st, impl->prob.kind == Kind::C2C, false, 1.f);
+}
 }  // namespace gfft
 
 extern "C" {

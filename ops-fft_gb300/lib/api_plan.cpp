@@ -83,6 +83,10 @@ aclfftResult check_sizes(const aclfftHandle_t* p)
     return ACLFFT_SUCCESS;
 }
 
+}  // namespace
+
+namespace gfft {
+
 // Plans every call variant of the transform described by the handle on the
 // host (kernel steps, twiddle segments, workspace sizes); NULL on failure.
 PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
@@ -100,6 +104,7 @@ PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
     pr.batch = h->batch;
     pr.stride = h->rank == 1 ? h->stride[0] : 1;
     pr.prec = pr.kind == Kind::C2C && pr.rank == 1 ? h->precision : 0;
+    pr.hints = h->hints;
     impl->prob = pr;
     impl->auto_ws = h->auto_allocate;
     Problem adj = pr;
@@ -126,6 +131,12 @@ PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
     return impl;
 }
 
+}  // namespace gfft
+
+namespace {
+
+using gfft::plan_steps;
+
 // Plans every call variant of the transform described by the handle.
 aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
 {
@@ -148,6 +159,18 @@ aclfftResult plan_execution(aclfftHandle_t* h, size_t* workSize)
     h->impl = impl;
     if (workSize) *workSize = gfft::work_area_bytes(impl);
     return ACLFFT_SUCCESS;
+}
+
+// MakePlan tunes when the plan asked for it (aclfftSetAutotune) or
+// OPS_FFT_AUTOTUNE=1 is set; a tuning failure keeps the planner's choices.
+void maybe_autotune(aclfftHandle_t* h, size_t* workSize)
+{
+    static const bool env_on = [] {
+        const char* v = std::getenv("OPS_FFT_AUTOTUNE");
+        return v && v[0] == '1';
+    }();
+    if (!(h->autotune || env_on)) return;
+    if (gfft::autotune_plan(h) == ACLFFT_SUCCESS && workSize && h->impl) *workSize = gfft::work_area_bytes(h->impl);
 }
 
 }  // namespace
@@ -359,6 +382,7 @@ ACLFFT_API aclfftResult aclfftMakePlan1d(aclfftHandle plan, int nx, aclfftType t
     const aclfftResult r = plan_execution(plan, workSize);
     if (r != ACLFFT_SUCCESS) return r;
     plan->is_initialized = true;
+    maybe_autotune(plan, workSize);
     return ACLFFT_SUCCESS;
 }
 
@@ -386,6 +410,7 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     const aclfftResult r = plan_execution(plan, workSize);
     if (r != ACLFFT_SUCCESS) return r;
     plan->is_initialized = true;
+    maybe_autotune(plan, workSize);
     return ACLFFT_SUCCESS;
 }
 

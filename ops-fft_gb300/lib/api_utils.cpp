@@ -191,6 +191,8 @@ ACLFFT_API aclfftResult aclfftGetPlanInfo(aclfftHandle plan, aclfftPlanInfo* inf
     }
     info->twiddle_entries = plan->impl->tb.count;
     info->workspace_bytes = gfft::work_area_bytes(plan->impl);
+    info->tuned = plan->tuned;
+    info->tune_candidates = plan->tune_candidates;
     return ACLFFT_SUCCESS;
 }
 

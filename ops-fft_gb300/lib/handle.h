@@ -79,6 +79,18 @@ aclfftResult allocate_workspace(PlanImpl* p);
 // (aclfftGetSize1d/2d).
 aclfftResult estimate_work_area(const aclfftHandle_t* desc, size_t* bytes);
 
+// Plans the handle's transform on the host with the handle's hints (no
+// device state); NULL on failure with the reason in *why.
+PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why);
+
+// Launches the out-of-place primary step list of a device-ready plan on
+// `st` (forward direction, no scaling); 0 or a CUDA error.
+int launch_primary(PlanImpl* impl, void* in, void* out, cudaStream_t st);
+
+// Times the planner's candidate choices for a made plan and re-plans it
+// with the fastest (aclfftSetAutotune).
+aclfftResult autotune_plan(aclfftHandle_t* h);
+
 }  // namespace gfft
 
 struct aclfftHandle_t {
@@ -93,10 +105,15 @@ struct aclfftHandle_t {
     gfft::PlanImpl* impl;
     int32_t precision;    // aclfftPrecisionMode (extension)
     bool auto_allocate;   // aclfftSetAutoAllocation (default: the plan allocates its workspace)
+    int32_t autotune;     // aclfftSetAutotune: 0 off, 1 tune when made
+    gfft::PlanHints hints;  // planner choices (defaults, or the autotuner's)
+    int32_t tuned;        // 1 when `hints` came from the autotuner (timed or cached)
+    int32_t tune_candidates;  // candidates timed by the last tuning (0: cache hit)
 
     aclfftHandle_t()
         : rank(0), lengths{0, 0, 0}, stride{0, 0, 0}, batch(1), type(ACLFFT_C2C), normMode(0), stream(nullptr),
-          is_initialized(false), impl(nullptr), precision(0), auto_allocate(true)
+          is_initialized(false), impl(nullptr), precision(0), auto_allocate(true), autotune(0), tuned(0),
+          tune_candidates(0)
     {
     }
     ~aclfftHandle_t()

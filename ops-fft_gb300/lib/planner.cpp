@@ -178,6 +178,15 @@ int row_nbuf(int npass, int start, bool last_global)
 
 }  // namespace
 
+// Hints of the problem being planned (set by build_steps for its duration).
+thread_local const PlanHints* t_hints = nullptr;
+
+struct HintScope {
+    explicit HintScope(const PlanHints* h) : prev(t_hints) { t_hints = h; }
+    ~HintScope() { t_hints = prev; }
+    const PlanHints* prev;
+};
+
 // Largest lengths accepted by the generic kernels (checked exactly below).
 int row_max_length() { return 13312; }
 
@@ -187,6 +196,7 @@ bool codelets_enabled()
         const char* v = std::getenv("OPS_FFT_CODELETS");
         return !(v && v[0] == '0');
     }();
+    if (t_hints && t_hints->codelets == 0) return false;
     return on;
 }
 int col_max_length() { return 2048; }
@@ -197,6 +207,7 @@ bool clusters_enabled()
         const char* v = std::getenv("OPS_FFT_CLUSTER");
         return !(v && v[0] == '0');
     }();
+    if (t_hints && t_hints->cluster == 0) return false;
     return on;
 }
 
@@ -211,7 +222,9 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     // OPS_FFT_CODELET_VARIANT=k selects the k-th entry of this length
     // (tuning experiments); unset or absent, the first one
     const char* env_var = std::getenv("OPS_FFT_CODELET_VARIANT");
-    int id = gfft_codelet_find(L, env_var ? std::atoi(env_var) : 0);
+    int want = env_var ? std::atoi(env_var) : 0;
+    if (t_hints && t_hints->codelet_variant >= 0) want = t_hints->codelet_variant;
+    int id = gfft_codelet_find(L, want);
     if (id < 0) id = gfft_codelet_find(L, 0);
     if (id < 0) return false;
     int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
@@ -261,8 +274,8 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     // prefetch stages (tuning experiments); unset, the score below decides
     const char* env_ng = std::getenv("OPS_FFT_CODELET_NG");
     const char* env_ns = std::getenv("OPS_FFT_CODELET_NST");
-    const int force_ng = env_ng ? std::atoi(env_ng) : 0;
-    const int force_ns = env_ns ? std::atoi(env_ns) : 0;
+    const int force_ng = (t_hints && t_hints->codelet_ng > 0) ? t_hints->codelet_ng : (env_ng ? std::atoi(env_ng) : 0);
+    const int force_ns = (t_hints && t_hints->codelet_nst > 0) ? t_hints->codelet_nst : (env_ns ? std::atoi(env_ns) : 0);
     for (int nst = 2; nst <= 4; ++nst) {
         if (force_ns ? nst != force_ns : nst > 3) continue;
         const int64_t gb = align(64 + nst * stage_bytes, 128);
@@ -577,7 +590,7 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st, i
 {
     if (!clusters_enabled() || n > 0x7fffffff) return false;
     const char* env_c = std::getenv("OPS_FFT_CLUSTER_C");
-    const int want_c = env_c ? std::atoi(env_c) : 0;
+    const int want_c = (t_hints && t_hints->cluster_c > 0) ? t_hints->cluster_c : (env_c ? std::atoi(env_c) : 0);
     int C = 0, Q = 0, P = 0, Q0 = 0, P0 = 0, nt = 0, smem = 0;
     const int kid = gfft_cluster_lookup(n, want_c, &C, &Q, &P, &Q0, &P0, &nt, &smem);
     if (kid < 0) return false;
@@ -611,6 +624,7 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st, i
 bool cluster_for_batch(int64_t n, int64_t batch)
 {
     if (n > 4096) return true;
+    if (t_hints && t_hints->cluster == 1) return true;
     const char* v = std::getenv("OPS_FFT_CLUSTER_MAXBATCH");
     return batch <= (v ? (int64_t)std::atoll(v) : (int64_t)1024);
 }
@@ -812,6 +826,7 @@ bool build_tc_c2c_steps(int64_t n, int64_t batch, int prec, bool inplace, Twiddl
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
                  int64_t& ws2_bytes)
 {
+    const HintScope hints(&p.hints);
     out = StepList{};
     ws_bytes = 0;
     ws2_bytes = 0;

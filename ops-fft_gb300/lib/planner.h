@@ -82,7 +82,25 @@ bool build_inner(int L, const std::vector<int>& radices, int nthr, TwiddleBuilde
 // receive the device workspace the steps need.
 enum class Kind { C2C, R2C, C2R };
 
+// Choices that override the planner's defaults for one plan (the plan
+// autotuner sets them; the default values keep the static rules and the
+// OPS_FFT_* environment knobs).
+struct PlanHints {
+    int codelet_variant = -1;  // k-th specialised build of the length
+    int codelet_ng = 0;        // transform groups per CTA of a codelet
+    int codelet_nst = 0;       // input prefetch stages of a codelet
+    int codelets = -1;         // 0: no specialised row kernels
+    int cluster = -1;          // 0: no cluster kernels; 1: clusters wherever a configuration exists
+    int cluster_c = 0;         // cluster size
+    bool operator==(const PlanHints& o) const
+    {
+        return codelet_variant == o.codelet_variant && codelet_ng == o.codelet_ng && codelet_nst == o.codelet_nst &&
+               codelets == o.codelets && cluster == o.cluster && cluster_c == o.cluster_c;
+    }
+};
+
 struct Problem {
+    PlanHints hints;
     Kind kind = Kind::C2C;
     int rank = 1;
     int64_t n0 = 1, n1 = 1;  // 1D: n0 = N. 2D: n0 = nx (slow), n1 = ny (fast)
