@@ -53,7 +53,7 @@ FALLBACK_HBM_GBS = 6800.0
 # the algorithmic read+write bytes.
 NCU_TRAFFIC = {
     ("cfg2", "dominant"): 52756480,  # R2C N=3000 batch=4096: 49.21 MB read + 3.54 MB written
-    ("cfg1", "dominant"): 8426752,   # C2C 4096 x 256 on 4-CTA clusters: 8.43 MB read (the 16.8 MB of data fit in L2)
+    ("cfg1", "dominant"): None,      # C2C 4096 x 256 now runs on the row codelet: not captured yet
     ("cfg3", "dominant"): 68792064,  # TF32x3 N=65536 x 64, both passes: 67.19 MB read + 1.60 MB written
     ("cfg4", "dominant"): 970750000,  # 2D forward: row pass 268.5 + 214.7 MB, column-tile pass 268.5 + 219.0 MB
     ("long", "dominant"): 487250944,  # C2C 65536 x 512 on 16-CTA clusters: 268.73 MB read + 218.52 MB written

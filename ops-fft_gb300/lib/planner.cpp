@@ -618,15 +618,17 @@ bool make_cluster_step(int64_t n, int64_t batch, TwiddleBuilder& tb, Step& st, i
 }
 
 // Lengths that a row kernel holds in one thread group (n <= 4096) run on a
-// cluster only when the batch is too small to fill the GPU with one group
-// per transform (at most OPS_FFT_CLUSTER_MAXBATCH transforms, default 1024);
-// longer lengths always prefer a cluster.
+// cluster only for batches of at most OPS_FFT_CLUSTER_MAXBATCH transforms
+// (default 0: never) or when the autotuner chose it; longer lengths always
+// prefer a cluster.  Measured C2C 4096 (us, cluster vs row codelet): b = 8
+// 3.57 / 3.62, 64 4.50 / 3.70, 256 7.04 / 5.22, 1024 18.5 / 16.1; R2C 8192
+// b = 64 5.44 / 4.17, 256 9.16 / 7.02.
 bool cluster_for_batch(int64_t n, int64_t batch)
 {
     if (n > 4096) return true;
     if (t_hints && t_hints->cluster == 1) return true;
     const char* v = std::getenv("OPS_FFT_CLUSTER_MAXBATCH");
-    return batch <= (v ? (int64_t)std::atoll(v) : (int64_t)1024);
+    return batch <= (v ? (int64_t)std::atoll(v) : (int64_t)0);
 }
 
 // Strided-axis transform as a list of column passes with buffer routing.

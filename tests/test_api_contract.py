@@ -465,6 +465,9 @@ def test_codelet_variants_and_cluster_choices_stay_in_bounds(variant, monkeypatc
             for b in (7, 1500):
                 with A.Plan.plan1d(n, typ, b) as p:
                     assert p.check() == "ok"
+    with A.Plan.plan1d(4096, A.C2C, 256) as p:       # default: the row codelet at every batch
+        assert p.info().cluster_ctas == 0 and p.check() == "ok"
+    monkeypatch.setenv("OPS_FFT_CLUSTER_MAXBATCH", "1024")
     for b, want in ((1024, True), (1025, False)):
         with A.Plan.plan1d(4096, A.C2C, b) as p:
             assert (p.info().cluster_ctas > 0) == want
