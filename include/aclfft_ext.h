@@ -80,8 +80,8 @@ ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* grad
  * stream; results are identical to scaling gradOut first and calling
  * aclfftExecR2CAdjoint.  Available for even nx whose adjoint runs as one
  * specialised row launch (aclfftGetPlanInfo: nsteps == 1 and kernel >= 0;
- * e.g. nx = 1024, 2048, 3000, 4096, and 8192 above batch 1024, where the
- * thread-block-cluster kernel hands over to the row kernel);
+ * e.g. nx = 1024, 2048, 3000, 4096, 8192; longer even lengths run on
+ * thread-block clusters or column passes);
  * ACLFFT_NOT_IMPLEMENTED otherwise. */
 ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const aclfftComplex* gradOut,
                                                      const aclfftReal* weights, aclfftReal* gradIn);

@@ -568,7 +568,7 @@ def _unit_root_fp32(m, M):
     return (cr - 1j * sr).astype(np.complex64)
 
 
-@pytest.mark.parametrize("n,b", [(3000, 64), (1024, 37), (2048, 5), (8192, 1100)])
+@pytest.mark.parametrize("n,b", [(3000, 64), (1024, 37), (2048, 5), (8192, 3), (8192, 1100)])
 def test_weighted_r2c_adjoint(n, b):
     """aclfftExecR2CAdjointWeighted(X, 2w) = dL/dx of L = sum(w*|X|^2),
     X = R2C(x): bit-identical to scaling X by 2w first and calling the plain
@@ -598,7 +598,7 @@ def test_weighted_r2c_adjoint(n, b):
 
 def test_weighted_r2c_adjoint_domain():
     dev = _dev()
-    for n, b in ((65536, 2), (999, 3), (1 << 20, 1), (8192, 3)):   # cluster, odd, column passes, cluster
+    for n, b in ((65536, 2), (999, 3), (1 << 20, 1), (16384, 4)):   # cluster, odd, column passes, cluster
         X = torch.zeros((b, n // 2 + 1), dtype=torch.complex64, device=dev)
         w = torch.ones((b, n // 2 + 1), dtype=torch.float32, device=dev)
         g = torch.empty((b, n), dtype=torch.float32, device=dev)
