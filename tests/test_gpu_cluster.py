@@ -185,11 +185,12 @@ def test_cluster_real_adjoints_vs_torch():
 
 
 def test_short_lengths_use_clusters_only_in_small_batches(monkeypatch):
-    # N = 4096 C2C and N = 8192 R2C: a cluster per transform for small
-    # batches, the one-group-per-transform row kernel above the batch limit;
-    # both give the FP64 result
-    for kind, n, b, lim, want in [(A.C2C, 4096, 256, None, True), (A.C2C, 4096, 256, "100", False),
-                                  (A.R2C, 8192, 64, None, True), (A.R2C, 8192, 64, "32", False)]:
+    # N = 4096 C2C and N = 8192 R2C: the row codelet by default; a cluster
+    # per transform at or below OPS_FFT_CLUSTER_MAXBATCH; both give the FP64
+    # result
+    for kind, n, b, lim, want in [(A.C2C, 4096, 256, None, False), (A.C2C, 4096, 256, "256", True),
+                                  (A.C2C, 4096, 256, "100", False), (A.R2C, 8192, 64, None, False),
+                                  (A.R2C, 8192, 64, "64", True), (A.R2C, 8192, 64, "32", False)]:
         if lim is None:
             monkeypatch.delenv("OPS_FFT_CLUSTER_MAXBATCH", raising=False)
         else:
