@@ -340,84 +340,10 @@ void build_items(aclfftRaggedPlan_t* p)
                      });
     for (auto& it : p2) it.need = np1[it.xform];
     for (auto& it : post) it.need = np1[it.xform] + np2[it.xform];
-    // Queue order.  Every wait must be on items queued earlier (they are
-    // claimed, hence running, before the waiter): a long transform's P2
-    // items follow all its P1 items, its POST item all its P2 items.  With
-    // OPS_FFT_RAGGED_LAG = 0 all P1 items come first, then the on-chip
-    // items, then all P2 and POST items; the workspace written by the P1
-    // steps of all long transforms (hundreds of MB) is then evicted from the
-    // L2 before the P2 steps read it.  With a lag of K items (default 4096),
-    // a transform's P2 items are released K items after its last P1 item
-    // and its POST item K items after its last P2 item, with the on-chip
-    // items spread between the long transforms, so the workspace in flight
-    // stays within the L2 and the waits are short.
-    static const int64_t lag = [] {
-        const char* v = std::getenv("OPS_FFT_RAGGED_LAG");
-        return v ? std::max<int64_t>(0, std::atoll(v)) : (int64_t)4096;
-    }();
-    if (lag == 0) {
-        p->items.insert(p->items.end(), p1.begin(), p1.end());
-        for (auto& s : singles) p->items.push_back(s.second);
-        p->items.insert(p->items.end(), p2.begin(), p2.end());
-        p->items.insert(p->items.end(), post.begin(), post.end());
-    } else {
-        // group each long transform's items (p1/p2/post are in transform order)
-        struct Group {
-            std::vector<RagItem> p1, p2, post;
-        };
-        std::vector<Group> groups;
-        std::vector<int> gidx(p->count, -1);
-        for (auto* list : {&p1, &p2, &post}) {
-            for (const RagItem& it : *list) {
-                int& gi = gidx[it.xform];
-                if (gi < 0) {
-                    gi = (int)groups.size();
-                    groups.emplace_back();
-                }
-                Group& g = groups[gi];
-                (list == &p1 ? g.p1 : (list == &p2 ? g.p2 : g.post)).push_back(it);
-            }
-        }
-        // pending releases: (position from which they may be queued, items)
-        std::vector<std::pair<int64_t, std::vector<RagItem>>> pend;
-        size_t next_single = 0;
-        auto flush = [&](bool all) {
-            // queue every pending batch whose release position is reached
-            // (all: everything, in release order)
-            for (size_t i = 0; i < pend.size();) {
-                if (all || pend[i].first <= (int64_t)p->items.size()) {
-                    std::vector<RagItem> batch = std::move(pend[i].second);
-                    pend.erase(pend.begin() + (long)i);
-                    const int64_t end_pos = (int64_t)p->items.size() + (int64_t)batch.size();
-                    // a P2 batch releases its transform's POST item
-                    if (!batch.empty() && batch.front().kind == RAG_P2) {
-                        const Group& g = groups[gidx[batch.front().xform]];
-                        if (!g.post.empty()) pend.push_back({end_pos + lag, g.post});
-                    }
-                    p->items.insert(p->items.end(), batch.begin(), batch.end());
-                    i = 0;
-                } else {
-                    ++i;
-                }
-            }
-        };
-        for (size_t gi = 0; gi < groups.size(); ++gi) {
-            const Group& g = groups[gi];
-            p->items.insert(p->items.end(), g.p1.begin(), g.p1.end());
-            pend.push_back({(int64_t)p->items.size() + lag, g.p2});
-            // spread the on-chip items evenly between the long transforms
-            const size_t left = groups.size() - gi;
-            const size_t take = (singles.size() - next_single + left - 1) / left;
-            for (size_t k = 0; k < take && next_single < singles.size(); ++k)
-                p->items.push_back(singles[next_single++].second);
-            flush(false);
-        }
-        for (; next_single < singles.size(); ++next_single) {
-            p->items.push_back(singles[next_single].second);
-            flush(false);
-        }
-        flush(true);
-    }
+    p->items.insert(p->items.end(), p1.begin(), p1.end());
+    for (auto& s : singles) p->items.push_back(s.second);
+    p->items.insert(p->items.end(), p2.begin(), p2.end());
+    p->items.insert(p->items.end(), post.begin(), post.end());
     p->smem = 16;
     for (auto& cp : p->classes) p->smem = std::max(p->smem, class_smem(cp.dev));
 }
