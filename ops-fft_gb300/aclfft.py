@@ -252,6 +252,12 @@ class Plan:
         _check(lib().aclfftPlan2d(ctypes.byref(h), batch, nx, ny, type_), "aclfftPlan2d")
         return cls(h.value)
 
+    @classmethod
+    def plan3d(cls, nx: int, ny: int, nz: int, type_: int = C2C) -> "Plan":
+        h = ctypes.c_void_p()
+        _check(lib().aclfftPlan3d(ctypes.byref(h), nx, ny, nz, type_), "aclfftPlan3d")
+        return cls(h.value)
+
     def set_stream(self, stream) -> None:
         s = getattr(stream, "cuda_stream", stream)
         _check(lib().aclfftSetStream(self.handle, ctypes.c_void_p(int(s) if s else None)), "aclfftSetStream")

@@ -74,7 +74,9 @@ aclfftResult drain_error_word(PlanImpl* impl, cudaStream_t st, int* flags_out)
 
 double points(const aclfftHandle_t* h)
 {
-    return h->rank == 2 ? (double)h->lengths[0] * (double)h->lengths[1] : (double)h->lengths[0];
+    double n = 1.0;
+    for (int a = 0; a < h->rank; ++a) n *= (double)h->lengths[a];
+    return n;
 }
 
 float norm_scale(const aclfftHandle_t* h, bool backward_like)
@@ -375,14 +377,23 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     return drain_error_word(impl, st, nullptr);
 }
 
+// Rows along the fastest axis (batch x the slower axes) and that axis' length.
+size_t outer_rows(const aclfftHandle_t* h)
+{
+    size_t r = (size_t)h->batch;
+    for (int a = 0; a + 1 < h->rank; ++a) r *= (size_t)h->lengths[a];
+    return r;
+}
+size_t last_len(const aclfftHandle_t* h) { return (size_t)h->lengths[h->rank - 1]; }
+
 size_t complex_elems(const aclfftHandle_t* h)
 {
-    if (h->rank == 2) return (size_t)h->batch * h->lengths[0] * h->lengths[1];
+    if (h->rank >= 2) return outer_rows(h) * last_len(h);
     return (size_t)h->batch * (size_t)h->lengths[0] * (size_t)(h->stride[0] > 1 ? h->stride[0] : 1);
 }
 
-size_t real_elems(const aclfftHandle_t* h) { return (size_t)h->batch * (size_t)h->lengths[0]; }
-size_t half_elems(const aclfftHandle_t* h) { return (size_t)h->batch * (size_t)(h->lengths[0] / 2 + 1); }
+size_t real_elems(const aclfftHandle_t* h) { return outer_rows(h) * last_len(h); }
+size_t half_elems(const aclfftHandle_t* h) { return outer_rows(h) * (last_len(h) / 2 + 1); }
 
 #define EXEC_PLAN_CHECKS(plan, a, b, expected)                                \
     ACLFFT_CHECK_NULL(plan);                                                  \
@@ -410,7 +421,7 @@ ACLFFT_API aclfftResult aclfftExecC2C(aclfftHandle plan, aclfftComplex* idata, a
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_C2C);
     ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
-    if (plan->rank != 1 && plan->rank != 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     const size_t bytes = complex_elems(plan) * 8;
     const bool inv = direction == ACLFFT_BACKWARD;
     return exec_common(plan, 0, idata, odata, {bytes, bytes}, true, inv, inv);
@@ -419,14 +430,14 @@ ACLFFT_API aclfftResult aclfftExecC2C(aclfftHandle plan, aclfftComplex* idata, a
 ACLFFT_API aclfftResult aclfftExecR2C(aclfftHandle plan, aclfftReal* idata, aclfftComplex* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_R2C);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false, false);
 }
 
 ACLFFT_API aclfftResult aclfftExecC2R(aclfftHandle plan, aclfftComplex* idata, aclfftReal* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_C2R);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false, true);
 }
 
@@ -435,7 +446,7 @@ ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* g
 {
     EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_C2C);
     ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
-    if (plan->rank != 1 && plan->rank != 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     const size_t bytes = complex_elems(plan) * 8;
     const bool primary_inv = direction == ACLFFT_BACKWARD;
     // adjoint of direction d is direction -d with the primary's scale
@@ -445,7 +456,7 @@ ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* g
 ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftReal* gradIn)
 {
     EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_R2C);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 2, gradOut, gradIn, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false,
                        false);
 }
@@ -496,7 +507,7 @@ ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const ac
 ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn)
 {
     EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_C2R);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 2, gradOut, gradIn, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false,
                        true);
 }

@@ -14,8 +14,13 @@
 //   aclfftDestroy      lib/fft_plan_destroy_api.cpp:24-40
 // Deliberate differences: MakePlan also plans the GPU execution (radix
 // sequence, twiddles generated on the GPU, workspace), *workSize reports the
-// workspace the plan owns, and 2D plans accept any C2C size (the reference
-// only has {32,64,128}^2 kernels and returns ACLFFT_NOT_SUPPORTED otherwise).
+// workspace the plan owns, 2D plans accept any C2C size (the reference only
+// has {32,64,128}^2 kernels and returns ACLFFT_NOT_SUPPORTED otherwise) and
+// R2C/C2R (the reference rejects them until its 2D real path lands,
+// lib/fft_plan_init_api.cpp:200-209), and 3D plans exist for C2C (the
+// reference's MakePlan3d returns ACLFFT_NOT_IMPLEMENTED, :250-254).  Double
+// precision (Z2Z/D2Z/Z2D) is rejected at plan time at every rank, as in the
+// reference's 1D and 2D entries.
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -100,7 +105,8 @@ PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
     pr.rank = h->rank;
     pr.kind = h->type == ACLFFT_C2C ? Kind::C2C : (h->type == ACLFFT_R2C ? Kind::R2C : Kind::C2R);
     pr.n0 = h->lengths[0];
-    pr.n1 = h->rank == 2 ? h->lengths[1] : 1;
+    pr.n1 = h->rank >= 2 ? h->lengths[1] : 1;
+    pr.n2 = h->rank == 3 ? h->lengths[2] : 1;
     pr.batch = h->batch;
     pr.stride = h->rank == 1 ? h->stride[0] : 1;
     pr.prec = pr.kind == Kind::C2C && pr.rank == 1 ? h->precision : 0;
@@ -395,7 +401,7 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) {
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
         GFFT_LOG("aclfftMakePlan2d: type=%d has no 2D execution implementation yet", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -414,16 +420,34 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     return ACLFFT_SUCCESS;
 }
 
+// 3D C2C of one nx x ny x nz volume (nz fastest), the reference's signature
+// (include/cann_ops_fft.h:260; no batch argument).
 ACLFFT_API aclfftResult aclfftMakePlan3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
                                          size_t* workSize)
 {
-    (void)plan;
-    (void)nx;
-    (void)ny;
-    (void)nz;
-    (void)type;
-    (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_PARAM(!plan->is_initialized, ACLFFT_INVALID_VALUE);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) {
+        GFFT_LOG("aclfftMakePlan3d: type=%d has no 3D execution implementation", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
+    plan->rank = 3;
+    plan->lengths[0] = nx;
+    plan->lengths[1] = ny;
+    plan->lengths[2] = nz;
+    plan->batch = 1;
+    plan->type = type;
+    plan->stride[0] = plan->stride[1] = plan->stride[2] = 1;
+    if (check_sizes(plan) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    const aclfftResult r = plan_execution(plan, workSize);
+    if (r != ACLFFT_SUCCESS) return r;
+    plan->is_initialized = true;
+    maybe_autotune(plan, workSize);
+    return ACLFFT_SUCCESS;
 }
 
 ACLFFT_API aclfftResult aclfftPlan1d(aclfftHandle* plan, int nx, aclfftType type, int batch, int dimType)
@@ -455,7 +479,7 @@ ACLFFT_API aclfftResult aclfftPlan2d(aclfftHandle* plan, int batch, int nx, int 
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) {
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
         GFFT_LOG("aclfftPlan2d: type=%d has no 2D execution implementation yet", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -476,6 +500,10 @@ ACLFFT_API aclfftResult aclfftPlan3d(aclfftHandle* plan, int nx, int ny, int nz,
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) {
+        GFFT_LOG("aclfftPlan3d: type=%d has no 3D execution implementation", (int)type);
+        return ACLFFT_NOT_SUPPORTED;
+    }
     aclfftResult r = aclfftCreate(plan);
     if (r != ACLFFT_SUCCESS) return r;
     r = aclfftMakePlan3d(*plan, nx, ny, nz, type, nullptr);
@@ -524,7 +552,7 @@ ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclff
     ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) return ACLFFT_NOT_SUPPORTED;
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) return ACLFFT_NOT_SUPPORTED;
     aclfftHandle_t d;
     d.rank = 2;
     d.lengths[0] = nx;
@@ -539,8 +567,23 @@ ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclff
 ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
                                         size_t* workSize)
 {
-    (void)plan; (void)nx; (void)ny; (void)nz; (void)type; (void)workSize;
-    return ACLFFT_NOT_IMPLEMENTED;  // no 3D transforms (aclfftMakePlan3d is a stub too)
+    ACLFFT_CHECK_NULL(plan);
+    ACLFFT_CHECK_NULL(workSize);
+    ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
+    ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
+    if (type != ACLFFT_C2C) return ACLFFT_NOT_SUPPORTED;
+    aclfftHandle_t d;
+    d.rank = 3;
+    d.lengths[0] = nx;
+    d.lengths[1] = ny;
+    d.lengths[2] = nz;
+    d.stride[0] = d.stride[1] = d.stride[2] = 1;
+    d.batch = 1;
+    d.type = type;
+    if (check_sizes(&d) != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
+    return gfft::estimate_work_area(&d, workSize);
 }
 
 ACLFFT_API aclfftResult aclfftGetSize(aclfftHandle plan, size_t* workSize)

@@ -92,7 +92,8 @@ std::string cache_key(const aclfftHandle_t* h)
         if (c == ' ') c = '_';
     std::ostringstream os;
     os << name << ':' << prop.multiProcessorCount << ':' << (int)h->type << ':' << h->rank << ':' << h->lengths[0]
-       << ':' << (h->rank == 2 ? h->lengths[1] : 1) << ':' << h->batch << ':' << h->stride[0] << ':' << h->precision;
+       << ':' << (h->rank >= 2 ? h->lengths[1] : 1) << ':' << (h->rank == 3 ? h->lengths[2] : 1) << ':' << h->batch
+       << ':' << h->stride[0] << ':' << h->precision;
     return os.str();
 }
 
@@ -229,10 +230,12 @@ aclfftResult autotune_plan(aclfftHandle_t* h)
     std::memcpy(trial.stride, h->stride, sizeof trial.stride);
     trial.type = h->type;
     trial.precision = h->precision;
-    const int64_t pts = (int64_t)h->lengths[0] * (h->rank == 2 ? h->lengths[1] : 1);
-    const int64_t in_per = pts * (h->type == ACLFFT_R2C ? 4 : 8);
-    const int64_t out_per = h->type == ACLFFT_C2C ? pts * 8
-                          : (h->type == ACLFFT_R2C ? ((int64_t)h->lengths[0] / 2 + 1) * 8 : pts * 4);
+    int64_t pts = 1;
+    for (int a = 0; a < h->rank; ++a) pts *= h->lengths[a];
+    const int64_t last = h->lengths[h->rank - 1];
+    const int64_t half = pts / last * (last / 2 + 1);  // bins of one half spectrum
+    const int64_t in_per = h->type == ACLFFT_C2C ? pts * 8 : (h->type == ACLFFT_R2C ? pts * 4 : half * 8);
+    const int64_t out_per = h->type == ACLFFT_C2C ? pts * 8 : (h->type == ACLFFT_R2C ? half * 8 : pts * 4);
     const int64_t cap = std::max<int64_t>(1, ((int64_t)256 << 20) / std::max<int64_t>(in_per, 1));
     trial.batch = (int32_t)std::min<int64_t>(h->batch, cap);
     const int64_t in_bytes = in_per * trial.batch;

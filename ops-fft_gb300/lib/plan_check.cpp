@@ -344,14 +344,18 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
     }
     PlanImpl* impl = plan->impl;
     const Problem& p = impl->prob;
-    int64_t cbytes, rbytes, hbytes;
+    // rows along the fastest axis and that axis' length
+    int64_t outer = p.batch, last = p.n0;
     if (p.rank == 2) {
-        cbytes = p.batch * p.n0 * p.n1 * 8;
-    } else {
-        cbytes = p.batch * p.n0 * std::max<int64_t>(p.stride, 1) * 8;
+        outer *= p.n0;
+        last = p.n1;
+    } else if (p.rank == 3) {
+        outer *= p.n0 * p.n1;
+        last = p.n2;
     }
-    rbytes = p.batch * p.n0 * 4;
-    hbytes = p.batch * (p.n0 / 2 + 1) * 8;
+    const int64_t cbytes = p.rank == 1 ? p.batch * p.n0 * std::max<int64_t>(p.stride, 1) * 8 : outer * last * 8;
+    const int64_t rbytes = outer * last * 4;
+    const int64_t hbytes = outer * (last / 2 + 1) * 8;
     for (int v = 0; v < 4; ++v) {
         const StepList& sl = impl->lists[v];
         if (!sl.supported) continue;

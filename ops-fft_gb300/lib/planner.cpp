@@ -842,26 +842,98 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
     auto need_ws = [&](int64_t bytes) { ws_bytes = std::max(ws_bytes, bytes); };
     auto need_ws2 = [&](int64_t bytes) { ws2_bytes = std::max(ws2_bytes, bytes); };
 
-    if (p.rank == 2) {
-        if (p.kind != Kind::C2C) return unsupported("2D supports C2C only");
-        const int64_t nx = p.n0, ny = p.n1;
-        if (!length_supported(nx) || !length_supported(ny)) return unsupported("2D length has a prime factor > 47");
-        const int64_t bytes = p.batch * nx * ny * 8;
-        // rows (contiguous, length ny) then columns (length nx, stride ny)
-        bool spare = false;
-        if (ny <= row_max_length() && row_feasible((int)ny, IO_C2C)) {
-            Step st;
-            if (!make_row_step((int)ny, p.batch * nx, ny, ny, IO_C2C, 0, WEIGHT_NONE, tb, st)) return false;
-            st.src = IN;
-            st.dst = BUF_OUT;
-            out.steps.push_back(st);
-        } else if (!make_axis_steps(ny, 1, p.batch * nx, ny, IN, BUF_OUT, BUF_WS, cap, tb, out.steps, spare)) {
-            return unsupported("2D row length not decomposable");
+    if (p.rank == 2 || p.rank == 3) {
+        const int nd = p.rank;
+        const int64_t dims[3] = {p.n0, p.n1, p.rank == 3 ? p.n2 : 1};
+        for (int a = 0; a < nd; ++a)
+            if (!length_supported(dims[a])) return unsupported("multi-dimensional length has a prime factor > 47");
+        const int64_t last = dims[nd - 1];
+        int64_t outer = p.batch;  // rows along the fastest axis
+        for (int a = 0; a + 1 < nd; ++a) outer *= dims[a];
+
+        if (p.kind == Kind::C2C) {
+            // one transform per axis, fastest first: the first pass reads the
+            // input, every later pass works on the output (strided columns)
+            const int64_t bytes = outer * last * 8;
+            int cur = IN;
+            int64_t S = 1;
+            for (int a = nd - 1; a >= 0; --a) {
+                const int64_t n = dims[a];
+                const int64_t items = outer * last / (n * S);
+                bool spare = false;
+                if (n > 1) {
+                    if (S == 1 && n <= row_max_length() && row_feasible((int)n, IO_C2C)) {
+                        Step st;
+                        if (!make_row_step((int)n, items, n, n, IO_C2C, 0, WEIGHT_NONE, tb, st)) return false;
+                        st.src = cur;
+                        st.dst = BUF_OUT;
+                        out.steps.push_back(st);
+                    } else if (!make_axis_steps(n, S, items, n * S, cur, BUF_OUT, BUF_WS, cap, tb, out.steps, spare)) {
+                        return unsupported("multi-dimensional axis length not decomposable");
+                    }
+                    cur = BUF_OUT;
+                }
+                if (spare) need_ws(bytes);
+                S *= n;
+            }
+            if (out.steps.empty() && IN != BUF_OUT) {  // every length 1: a copy
+                Step cp;
+                cp.kind = Step::COPY;
+                cp.copy_bytes = bytes;
+                cp.src = IN;
+                cp.dst = BUF_OUT;
+                out.steps.push_back(cp);
+            }
+            return true;
         }
-        if (spare) need_ws(bytes);
-        if (!make_axis_steps(nx, ny, p.batch, nx * ny, BUF_OUT, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
-            return unsupported("2D column length not decomposable");
-        if (spare) need_ws(bytes);
+
+        // real 2D: rows of length ny through the 1D real planner, columns
+        // (length nx, stride ny/2+1) over the half spectrum
+        if (nd != 2) return unsupported("3D supports C2C only");
+        const int64_t nx = p.n0, ny = p.n1, nb = ny / 2 + 1;
+        const int64_t half_bytes = p.batch * nx * nb * 8;
+        Problem rows;
+        rows.hints = p.hints;
+        rows.kind = p.kind;
+        rows.n0 = ny;
+        rows.batch = p.batch * nx;
+        rows.weight = p.weight;
+        StepList sub;
+        int64_t sub_ws = 0, sub_ws2 = 0;
+        bool spare = false;
+        if (p.kind == Kind::R2C) {
+            if (!build_steps(rows, inplace, tb, sub, sub_ws, sub_ws2)) return false;
+            if (!sub.supported) return unsupported(sub.why.c_str());
+            out.steps = sub.steps;
+            need_ws(sub_ws);
+            need_ws2(sub_ws2);
+            if (nx > 1 &&
+                !make_axis_steps(nx, nb, p.batch, nx * nb, BUF_OUT, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
+                return unsupported("2D column length not decomposable");
+            if (spare) need_ws(half_bytes);
+            return true;
+        }
+        // C2R: backward column transforms of the half spectrum into the
+        // second work area (the input stays intact), then the real rows
+        const bool cols = nx > 1;
+        if (!build_steps(rows, cols ? false : inplace, tb, sub, sub_ws, sub_ws2)) return false;
+        if (!sub.supported) return unsupported(sub.why.c_str());
+        if (cols) {
+            if (!make_axis_steps(nx, nb, p.batch, nx * nb, IN, BUF_WS2, BUF_WS, cap, tb, out.steps, spare))
+                return unsupported("2D column length not decomposable");
+            out.steps.front().col.conj_in = 1;
+            out.steps.back().col.conj_out = 1;
+            need_ws2(half_bytes);
+            if (spare) need_ws(half_bytes);
+            for (Step& s : sub.steps) {
+                if (s.src == BUF_WS2 || s.dst == BUF_WS2)
+                    return unsupported("2D C2R rows of this length need a second work area of their own");
+                if (s.src == BUF_IN) s.src = BUF_WS2;
+            }
+        }
+        out.steps.insert(out.steps.end(), sub.steps.begin(), sub.steps.end());
+        need_ws(sub_ws);
+        need_ws2(sub_ws2);
         return true;
     }
 

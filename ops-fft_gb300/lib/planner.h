@@ -103,7 +103,7 @@ struct Problem {
     PlanHints hints;
     Kind kind = Kind::C2C;
     int rank = 1;
-    int64_t n0 = 1, n1 = 1;  // 1D: n0 = N. 2D: n0 = nx (slow), n1 = ny (fast)
+    int64_t n0 = 1, n1 = 1, n2 = 1;  // 1D: n0 = N. 2D: n0 = nx (slow), n1 = ny (fast). 3D: n0, n1, n2 = nx, ny, nz
     int64_t batch = 1;
     int64_t stride = 1;      // VERTICAL 1D: stride between samples (= batch), batch = 1
     int weight = WEIGHT_NONE;

@@ -160,6 +160,33 @@ def c2r(X, n: int) -> np.ndarray:
     return out
 
 
+def _c2c_axis(x, axis: int, sign: int) -> np.ndarray:
+    """Unscaled C2C along one axis through the C oracle (moved last, back)."""
+    y = np.moveaxis(np.asarray(x, dtype=np.complex128), axis, -1)
+    return np.moveaxis(c2c(y, sign), -1, axis)
+
+
+def r2c_2d(x) -> np.ndarray:
+    """2D real-to-complex over the last two axes of [..., nx, ny]: rows of
+    length ny to ny//2+1 bins, then forward C2C down the columns (length nx).
+    Composed from the pinned 1D oracles; the reference has no 2D real path
+    (lib/fft_plan_init_api.cpp:200-209 rejects it), numpy's rfft2 is the
+    independent cross-check in the oracle tests."""
+    return _c2c_axis(r2c(x), -2, -1)
+
+
+def c2r_2d(X, ny: int) -> np.ndarray:
+    """Unscaled 2D complex-to-real (nx * ny * irfft2): backward C2C down the
+    columns of the half spectrum, then rows of ny//2+1 bins to ny samples."""
+    return c2r(_c2c_axis(X, -2, +1), ny)
+
+
+def c2c_3d(x, sign: int = -1) -> np.ndarray:
+    """Unscaled 3D C2C over the last three axes (fastest first)."""
+    y = c2c(np.asarray(x, dtype=np.complex128), sign)
+    return _c2c_axis(_c2c_axis(y, -2, sign), -3, sign)
+
+
 def dft_bins(x, bins, sign: int = -1) -> np.ndarray:
     """Direct O(n) evaluation of a few bins of one transform (cross-check)."""
     x = np.ascontiguousarray(x, dtype=np.complex128).reshape(-1)

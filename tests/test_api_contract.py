@@ -96,9 +96,9 @@ def test_plan1d_error_codes_match_reference():
 
 
 def test_plan2d_error_codes_match_reference_within_its_domain():
-    """The reference only accepts {32,64,128}^2; elsewhere it returns
+    """The reference only accepts C2C of {32,64,128}^2; elsewhere it returns
     NOT_SUPPORTED where this library plans the transform (documented
-    widening).  Every other code must match."""
+    widening: any C2C size, and R2C/C2R).  Every other code must match."""
     ref = _ref_lib()
     mine = A.lib()
     for nx in (0, 32, 64, 128, 2048, 7):
@@ -112,9 +112,36 @@ def test_plan2d_error_codes_match_reference_within_its_domain():
                         ref.aclfftDestroy(h1)
                     if c == 0:
                         mine.aclfftDestroy(h2)
-                    if a == A.NOT_SUPPORTED and c == 0 and t == A.C2C:
+                    if a == A.NOT_SUPPORTED and c == 0 and t in (A.C2C, A.R2C, A.C2R):
                         continue
                     assert a == c, (b, nx, ny, t, a, c)
+
+
+def test_plan3d_error_codes_match_reference_outside_its_stub():
+    """The reference's MakePlan3d is a stub (NOT_IMPLEMENTED after Plan3d's
+    argument checks, lib/fft_plan_api.cpp:127-150); here C2C plans and the
+    other types are NOT_SUPPORTED.  Argument-check codes must match."""
+    ref = _ref_lib()
+    mine = A.lib()
+    for nx, ny, nz in ((0, 8, 8), (8, -1, 8), (8, 8, 0), (8, 8, 8), (1, 1, 1), (7, 64, 3000)):
+        for t in TYPES:
+            h1, h2 = ctypes.c_void_p(), ctypes.c_void_p()
+            a = ref.aclfftPlan3d(ctypes.byref(h1), nx, ny, nz, t)
+            c = mine.aclfftPlan3d(ctypes.byref(h2), nx, ny, nz, t)
+            if a == 0:
+                ref.aclfftDestroy(h1)
+            if c == 0:
+                mine.aclfftDestroy(h2)
+            if a == A.NOT_IMPLEMENTED:
+                assert c == (0 if t == A.C2C else A.NOT_SUPPORTED), (nx, ny, nz, t, c)
+                continue
+            assert a == c, (nx, ny, nz, t, a, c)
+    h = ctypes.c_void_p()
+    assert mine.aclfftCreate(ctypes.byref(h)) == 0
+    assert mine.aclfftMakePlan3d(h, 4, 4, 4, A.C2C, None) == 0
+    assert mine.aclfftMakePlan3d(h, 4, 4, 4, A.C2C, None) == A.INVALID_VALUE  # already made
+    mine.aclfftDestroy(h)
+    assert mine.aclfftMakePlan3d(None, 4, 4, 4, A.C2C, None) == A.INVALID_VALUE
 
 
 def test_exec_entry_checks_match_reference():
@@ -165,18 +192,18 @@ def test_makeplan_twice_and_create_null():
 
 def test_stubs_return_not_implemented():
     """Entries that stay stubs, as in the reference (lib/fft_utils_api.cpp,
-    lib/fft_exec_api.cpp:87-116): 3D, double precision and SetStride."""
+    lib/fft_exec_api.cpp:87-116): double precision and SetStride; 3D plans
+    of other types than C2C are NOT_SUPPORTED."""
     mine = A.lib()
     h = ctypes.c_void_p()
-    sz = ctypes.c_size_t()
-    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.C2C, ctypes.byref(sz)) == A.NOT_IMPLEMENTED
     assert mine.aclfftSetStride(h, 2) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecZ2Z(h, None, None, -1) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecD2Z(h, None, None) == A.NOT_IMPLEMENTED
     assert mine.aclfftExecZ2D(h, None, None) == A.NOT_IMPLEMENTED
-    hp = ctypes.c_void_p()
-    assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, A.C2C) == A.NOT_IMPLEMENTED
-    assert not hp.value
+    for t in (A.R2C, A.C2R, A.Z2Z):
+        hp = ctypes.c_void_p()
+        assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, t) == A.NOT_SUPPORTED
+        assert not hp.value
 
 
 def test_version_queries():
@@ -211,7 +238,10 @@ def test_work_area_queries():
     assert mine.aclfftGetSize1d(h, 64, 0x2B, 1, ctypes.byref(sz)) == A.INVALID_TYPE
     assert mine.aclfftGetSize1d(h, 64, A.Z2Z, 1, ctypes.byref(sz)) == A.NOT_SUPPORTED
     assert mine.aclfftGetSize1d(h, (1 << 27) + 1, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_SIZE
-    assert mine.aclfftGetSize2d(h, 64, 64, A.R2C, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize2d(h, 64, 64, A.Z2Z, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.R2C, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize3d(h, 8, 0, 8, A.C2C, ctypes.byref(sz)) == A.INVALID_SIZE
+    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.C2C, None) == A.INVALID_VALUE
     assert mine.aclfftGetSize(h, ctypes.byref(sz)) == A.INVALID_PLAN  # not made yet
     mine.aclfftDestroy(h)
     cases = [(4096, A.C2C, 256), (3000, A.R2C, 4096), (1024, A.C2R, 16), (1 << 20, A.C2C, 4), (1 << 25, A.R2C, 2),
@@ -227,9 +257,15 @@ def test_work_area_queries():
         assert est.value == made.value == sz.value, (n, t, b, est.value, made.value, sz.value)
         mine.aclfftDestroy(q)
     for nx, ny in ((2048, 2048), (64, 128), (7, 3000)):
+        for t in (A.C2C, A.R2C, A.C2R):
+            est = ctypes.c_size_t()
+            with A.Plan.plan2d(1, nx, ny, t) as p:
+                assert mine.aclfftGetSize2d(p.handle, nx, ny, t, ctypes.byref(est)) == 0
+                assert est.value == p.work_size()
+    for dims in ((64, 64, 64), (5, 3000, 7), (512, 512, 512)):
         est = ctypes.c_size_t()
-        with A.Plan.plan2d(1, nx, ny, A.C2C) as p:
-            assert mine.aclfftGetSize2d(p.handle, nx, ny, A.C2C, ctypes.byref(est)) == 0
+        with A.Plan.plan3d(*dims) as p:
+            assert mine.aclfftGetSize3d(p.handle, *dims, A.C2C, ctypes.byref(est)) == 0
             assert est.value == p.work_size()
     # a long transform needs a work area between its passes
     with A.Plan.plan1d(1 << 20, A.C2C, 4) as p:
@@ -348,10 +384,16 @@ def test_vertical_and_2d_launches_stay_in_bounds():
             with A.Plan.plan1d(n, A.C2C, b, A.VERTICAL) as p:
                 p.check()
     for nx, ny in ((32, 32), (64, 128), (128, 32), (2048, 2048), (7, 3000), (4096, 4096), (1, 5), (17, 19),
-                   (100000, 3), (3, 100000)):
-        with A.Plan.plan2d(2, nx, ny, A.C2C) as p:
-            if p.info().supported:
-                p.check()
+                   (100000, 3), (3, 100000), (1, 1), (5, 1), (2, 16384), (3, 1 << 20)):
+        for t in (A.C2C, A.R2C, A.C2R):
+            with A.Plan.plan2d(2, nx, ny, t) as p:
+                if p.info().supported:
+                    p.check()
+    for dims in ((1, 1, 1), (2, 2, 2), (64, 64, 64), (5, 3000, 7), (7, 5, 3000), (3000, 7, 5), (256, 256, 256),
+                 (1, 64, 1), (16, 1, 65536), (4, 5000, 6)):
+        with A.Plan.plan3d(*dims) as p:
+            assert p.info().supported, dims
+            p.check()
 
 
 def test_precision_mode_extension():

@@ -132,3 +132,33 @@ def test_long_row_oracle_agrees_with_c_oracle():
         x = rng.standard_normal((1, n))
         a, b = O.r2c(x), O.r2c_long_rows(x)
         assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-13
+
+
+@pytest.mark.parametrize("shape", [(1, 8, 6), (2, 7, 10), (3, 16, 15), (1, 1, 5), (2, 5, 1), (1, 30, 64)])
+def test_multidim_real_oracles_agree_with_numpy(shape):
+    """The 2D real oracles (composed from the pinned 1D C oracle) agree with
+    numpy's independent FP64 rfft2 / irfft2 to FP64 rounding, and the 2D C2C
+    oracle with the pinned fft2_d oracle."""
+    rng = np.random.default_rng(sum(shape))
+    x = rng.standard_normal(shape)
+    nx, ny = shape[-2:]
+    X = O.r2c_2d(x)
+    ref = np.fft.rfft2(x)
+    assert np.abs(X - ref).max() < 1e-12 * nx * ny
+    # C2R of a general half spectrum: only the real parts of the ny=0 and
+    # ny/2 bins of the column-transformed data enter (numpy's convention)
+    Y = rng.standard_normal(X.shape) + 1j * rng.standard_normal(X.shape)
+    y = O.c2r_2d(Y, ny)
+    assert np.abs(y - np.fft.irfft2(Y, s=(nx, ny)) * nx * ny).max() < 1e-11 * nx * ny
+    assert np.abs(O.c2r_2d(X, ny) - nx * ny * x).max() < 1e-10 * nx * ny
+    z = x + 1j * rng.standard_normal(shape)
+    assert np.abs(O._c2c_axis(O.c2c(z, -1), -2, -1) - O.c2c_2d(z, -1)).max() < 1e-12 * nx * ny
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 4), (5, 1, 7), (8, 8, 8), (1, 1, 1), (3, 30, 10)])
+def test_3d_oracle_agrees_with_numpy(shape):
+    rng = np.random.default_rng(sum(shape) + 1)
+    x = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    n = int(np.prod(shape))
+    assert np.abs(O.c2c_3d(x, -1) - np.fft.fftn(x)).max() < 1e-12 * n
+    assert np.abs(O.c2c_3d(x, +1) - np.fft.ifftn(x) * n).max() < 1e-12 * n

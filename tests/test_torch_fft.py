@@ -134,3 +134,48 @@ def test_plans_are_per_stream_and_threads_do_not_race(F):
     assert not errors, errors
     for i in range(2):
         assert _rel(results[i], exact[i]) <= REL
+
+
+@pytest.mark.parametrize("shape", [(3, 16, 12), (2, 9, 7), (1, 64, 1000)])
+def test_rfft2_irfft2_forward_and_gradient(F, shape):
+    """2D real wrappers: values against torch.fft.rfft2 / irfft2 and
+    gradients of L = sum w|rfft2(x)|^2 + sum v * irfft2(X) against FP64
+    autograd."""
+    nx, ny = shape[-2:]
+    rng = np.random.default_rng(nx + ny)
+    x = rng.standard_normal(shape)
+    w = rng.uniform(0, 1, shape[:-1] + (ny // 2 + 1,))
+    v = rng.standard_normal(shape)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda", requires_grad=True)
+    X = F.rfft2(xd)
+    y = F.irfft2(X, (nx, ny))
+    loss = (torch.tensor(w, dtype=torch.float32, device="cuda") * X.abs() ** 2).sum() + \
+        (torch.tensor(v, dtype=torch.float32, device="cuda") * y).sum()
+    loss.backward()
+    assert _rel(X.detach().cpu().numpy(), np.fft.rfft2(x)) <= REL
+    assert _rel(y.detach().cpu().numpy(), x * nx * ny) <= REL
+    xt = torch.tensor(x, requires_grad=True)
+    Xt = torch.fft.rfft2(xt)
+    yt = torch.fft.irfft2(Xt, s=(nx, ny)) * (nx * ny)
+    ((torch.tensor(w) * Xt.abs() ** 2).sum() + (torch.tensor(v) * yt).sum()).backward()
+    assert _rel(xd.grad.cpu().numpy(), xt.grad.numpy()) <= REL
+    with pytest.raises(ValueError):
+        F.irfft2(X, (nx, ny + 2))
+
+
+@pytest.mark.parametrize("inverse", [False, True])
+def test_fft2_fftn_forward_and_gradient(F, inverse):
+    rng = np.random.default_rng(int(inverse))
+    for shape, fn, tfn, axes in (((2, 12, 20), F.fft2, torch.fft.fft2, (-2, -1)),
+                                 ((3, 6, 10, 14), F.fftn, torch.fft.fftn, (-3, -2, -1))):
+        z = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        G = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        zd = torch.tensor(z, dtype=torch.complex64, device="cuda", requires_grad=True)
+        Z = fn(zd, inverse=inverse)
+        torch.real(torch.conj(torch.tensor(G, dtype=torch.complex64, device="cuda")) * Z).sum().backward()
+        npts = int(np.prod([shape[a] for a in axes]))
+        zt = torch.tensor(z, requires_grad=True)
+        Zt = (torch.fft.ifftn(zt, dim=axes) * npts) if inverse else tfn(zt, dim=axes)
+        torch.real(torch.conj(torch.tensor(G)) * Zt).sum().backward()
+        assert _rel(Z.detach().cpu().numpy(), Zt.detach().numpy()) <= REL, shape
+        assert _rel(zd.grad.cpu().numpy(), zt.grad.numpy()) <= REL, shape
