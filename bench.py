@@ -998,6 +998,53 @@ def extra_long_lengths(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak)
     return out
 
 
+def extra_multidim(torch, A, dev, stream, timer, nk, reps, warmup, peak):
+    """2D and 3D forms beyond the reference's 2D C2C of 32-128 squares: per
+    exec call on device buffers the median time, GB/s of one read of the
+    input plus one write of the output, its fraction of the measured HBM copy
+    peak, the launches per call, and cuFFT (torch.fft, unnormalised) on the
+    same shape for scale.  Inputs and outputs are above the L2 size."""
+    g = torch.Generator(device=dev).manual_seed(7)
+    b, nx = 8, 2048
+    xr = torch.rand((b, nx, nx), generator=g, device=dev) * 2 - 1
+    xc = torch.complex(xr, torch.rand((b, nx, nx), generator=g, device=dev) * 2 - 1)
+    yc = torch.empty_like(xc)
+    Xh = torch.empty((b, nx, nx // 2 + 1), dtype=torch.complex64, device=dev)
+    yr = torch.empty_like(xr)
+    v = torch.complex(torch.rand((512,) * 3, generator=g, device=dev), torch.rand((512,) * 3, generator=g, device=dev))
+    w = torch.empty_like(v)
+    cases = [
+        ("2D C2C 8x2048x2048", A.Plan.plan2d(b, nx, nx, A.C2C), lambda p: p.exec_c2c(xc, yc, A.FORWARD),
+         lambda: torch.fft.fft2(xc, out=yc), 2 * xc.numel() * 8),
+        ("2D R2C 8x2048x2048", A.Plan.plan2d(b, nx, nx, A.R2C), lambda p: p.exec_r2c(xr, Xh),
+         lambda: torch.fft.rfft2(xr, out=Xh), xr.numel() * 4 + Xh.numel() * 8),
+        ("2D C2R 8x2048x2048", A.Plan.plan2d(b, nx, nx, A.C2R), lambda p: p.exec_c2r(Xh, yr),
+         lambda: torch.fft.irfft2(Xh, s=(nx, nx), norm="forward", out=yr), xr.numel() * 4 + Xh.numel() * 8),
+        ("3D C2C 512^3", A.Plan.plan3d(512, 512, 512), lambda p: p.exec_c2c(v, w, A.FORWARD),
+         lambda: torch.fft.fftn(v, out=w), 2 * v.numel() * 8),
+    ]
+    out = {}
+    for name, plan, call, lib, byt in cases:
+        plan.set_stream(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                call(plan)
+                lib()
+        torch.cuda.synchronize()
+        t = timer(lambda i, p=plan, c=call: c(p), nk, reps) or timer.eager(lambda i, p=plan, c=call: c(p), nk, reps)
+        tl = timer(lambda i: lib(), nk, reps) or timer.eager(lambda i: lib(), nk, reps)
+        us = statistics.median(t) / nk * 1e3
+        us_lib = statistics.median(tl) / nk * 1e3
+        gbs = byt / (us / 1e6) / 1e9
+        out[name] = {"us": round(us, 1), "GB/s": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 3),
+                     "launches": plan.info().nsteps, "workspace_MB": round(plan.work_size() / 1e6, 1),
+                     "cufft_us": round(us_lib, 1)}
+        plan.destroy()
+    del xr, xc, yc, Xh, yr, v, w
+    torch.cuda.empty_cache()
+    return out
+
+
 def extra_autograd(torch, dev, stream, nk, reps, warmup):
     """The headline step through the torch.autograd wrappers (torch_fft):
     X = rfft(x), y = irfft(X, n), loss = sum(w*|X|^2), loss.backward() -
@@ -1204,6 +1251,8 @@ def main():
         extras["per_length_n4096_65536"] = extra_long_lengths(torch, A, dev, stream, timer, nk, max(5, reps // 4),
                                                               args.warmup, l2, peak)
         extras["autograd_step"] = extra_autograd(torch, dev, stream, nk, max(5, reps // 4), args.warmup)
+        extras["multidim_2d_3d"] = extra_multidim(torch, A, dev, stream, timer, nk, max(5, reps // 4), args.warmup,
+                                                  peak)
         wl = make_workload(args.workload, torch, A, dev, stream, 1)
 
     cpu = None

@@ -15,10 +15,14 @@
 //     the group leader NST slots ahead.  TPS is chosen so a slot is a 16-byte
 //     aligned, 16-byte multiple range (2 for rows of an odd number of float2);
 //   * pass p: thread owns NB_p = ceil(L/R_p / NTHR) butterflies
-//     j = tid + b*NTHR and holds their R_p inputs in registers; the passes
-//     run in place in one shared buffer per group (all reads of a pass finish
-//     before any write); the first pass reads the slot, the last pass writes
-//     HBM directly (or shared memory for the R2C post-process);
+//     j = tid + b*NTHR and holds their R_p inputs in registers; the first
+//     pass reads the slot, the last pass writes HBM directly (or shared
+//     memory for the R2C post-process).  Without a work buffer (nbuf 1) the
+//     passes run in place in the slot (all reads of a pass finish before any
+//     write: two group barriers per pass); with one (nbuf 2, ping-pong) they
+//     alternate between the slot and the group's work buffer, ending in the
+//     work buffer, so each pass needs one barrier and the slot is refilled
+//     as soon as the last pass that reads it is done;
 //   * twiddle tables and the real-data post-process twiddles are copied to
 //     shared memory once per CTA.
 // Every mbarrier wait is bounded (~2 s); on expiry the group records bit 0 in
@@ -107,10 +111,13 @@ __device__ __forceinline__ void group_sync(int id)
 
 // One in-place pass P of codelet S on the transform held in W (shared) or,
 // for P == 0 with from_slot, read from the slot copy through c.gload.
+// Win: input buffer (ignored when the pass reads the slot); Wout: output
+// buffer; sync_loaded: a group barrier between the loads and the stores
+// (in-place passes, and passes whose input buffer must be free afterwards).
 template <class S, int P, bool FC2R = false>
-__device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2 (&v)[S::E], const float2* tw,
-                                             int tw_off, bool from_slot, bool last_global, int bar_id,
-                                             const float2* post = nullptr)
+__device__ __forceinline__ void codelet_pass(const PipeCtx& c, const float2* Win, float2* Wout, float2 (&v)[S::E],
+                                             const float2* tw, int tw_off, bool from_slot, bool last_global,
+                                             bool sync_loaded, int bar_id, const float2* post = nullptr)
 {
     constexpr int R = S::R[P];
     constexpr int NS = S::ns(P);
@@ -171,7 +178,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
         } else {
             load_all([&](int i) { return c.st2[i]; });
         }
-        group_sync<S>(bar_id);  // the raw row and the padded work layout share the slot
+        if (sync_loaded) group_sync<S>(bar_id);  // e.g. the raw row and an in-slot output share the slot
     } else {
         sfor<NB>([&](auto bb) {
             constexpr int b = decltype(bb)::value;
@@ -179,11 +186,11 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
             if (FULL || j < NBF) {
                 sfor<R>([&](auto rr) {
                     constexpr int r = decltype(rr)::value;
-                    v[b * R + r] = W[cpad<S>(j + r * NBF)];
+                    v[b * R + r] = Win[cpad<S>(j + r * NBF)];
                 });
             }
         });
-        group_sync<S>(bar_id);  // in place: every read of this pass precedes any write
+        if (sync_loaded) group_sync<S>(bar_id);  // in place: every read of this pass precedes any write
     }
     // ---- twiddle + butterfly
     sfor<NB>([&](auto bb) {
@@ -239,7 +246,7 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
                 const int base = q * NS * R + k;
                 sfor<R>([&](auto rr) {
                     constexpr int r = decltype(rr)::value;
-                    W[cpad<S>(base + r * NS)] = v[b * R + r];
+                    Wout[cpad<S>(base + r * NS)] = v[b * R + r];
                 });
             }
         });
@@ -255,7 +262,9 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, float2* W, float2
 //                                  slots of stage_bytes.  A slot holds one
 //                                  transform: its raw input row at offset
 //                                  src % 16, then (in place, from offset 16)
-//                                  the padded work layout.
+//                                  the padded work layout WA; with nbuf 2
+//                                  the group's work buffer WB (lpad float2)
+//                                  follows at group offset smem_work.
 //
 // Slot fill: the row of transform t starts at src = in + t*row_bytes and is
 // placed at slot + (src % 16), so the 16-byte aligned superset
@@ -358,6 +367,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
     const float2* tw = stw - A.tw_lo;
     const float2* post = spost;
     const bool last_global = A.io_mode != IO_R2C_EVEN;
+    const bool pp = A.nbuf == 2;  // the group has a work buffer at gbase + smem_work
     float2 v[S::E];
     constexpr int NPP = (L / 2 + 1 + S::NTHR - 1) / S::NTHR;  // C2R pre-process pairs per thread
 
@@ -388,9 +398,10 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             for (int64_t i = tid; i < row_bytes / 4; i += S::NTHR) reinterpret_cast<float*>(row)[i] = __ldg(gs + i);
             group_sync<S>(bar_id);
         }
-        // work layout (padded, 16-byte aligned) overlaps the raw row: every
-        // pass reads all its inputs before it writes
-        float2* W = reinterpret_cast<float2*>(slots + (int64_t)s * A.stage_bytes + 16);
+        // work layouts (padded, 16-byte aligned): WA inside the slot (it
+        // overlaps the raw row), WB the group's work buffer (nbuf 2)
+        float2* WA = reinterpret_cast<float2*>(slots + (int64_t)s * A.stage_bytes + 16);
+        float2* WB = pp ? reinterpret_cast<float2*>(gbase + A.smem_work) : WA;
         PipeCtx c;
         c.L = L;
         c.nthr = S::NTHR;
@@ -399,8 +410,8 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         c.ok_io = true;
         c.pshift = S::PSHIFT;
         c.tw = tw;
-        c.sA = W;
-        c.sB = W;
+        c.sA = WA;
+        c.sB = WB;
         c.st2 = reinterpret_cast<const float2*>(row);
         c.st1 = reinterpret_cast<const float*>(row);
         c.mode = A.io_mode;
@@ -413,12 +424,37 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         c.out1 = reinterpret_cast<float*>(A.out) + t * A.out_dist;
         c.wl = A.wload ? A.wload + t * A.wdist : nullptr;
 
+        // the slot is free once no later stage reads it: refill it with the
+        // transform NST iterations ahead (group leader, after a group barrier
+        // that follows the last read of the slot)
+        bool refilled = false;
+        auto refill = [&]() {
+            refilled = true;
+            if (leader) {
+                const int64_t nt = gfirst + (it + NST) * gstride;
+                if (nt < A.ntf) {
+                    fence_proxy_async_smem();
+                    issue(s, nt);
+                }
+            }
+        };
+        // shared-writing stages: the C2R pre-process, then every pass but a
+        // last one that writes HBM.  With a work buffer, stage i writes WB
+        // when K-1-i is even (so the last one writes WB) and WA otherwise;
+        // without one, every stage runs in place in WA.
+        const bool pre = !FC2R && A.io_mode == IO_C2R_EVEN;
+        const int K = (pre ? 1 : 0) + S::NP - (last_global ? 1 : 0);
+        auto out_of = [&](int i) { return (pp && ((K - 1 - i) & 1) == 0) ? WB : WA; };
+        int stage = 0;
+        const float2* cur = WA;  // input of the next stage once the raw row is consumed
         bool from_slot = true;
-        if (!FC2R && A.io_mode == IO_C2R_EVEN) {
-            // pre-process pairs (k, L-k) in place:
+        if (pre) {
+            // pre-process pairs (k, L-k):
             //   Z'[k] = E + i*O,  E = X[k] + conj(X[L-k]),
             //   O = (X[k] - conj(X[L-k])) * conj(W_N^k), stored conjugated.
-            // All pairs are read into registers before any is written.
+            // All pairs are read into registers before any is written when
+            // the output overlaps the raw row.
+            float2* Wo = out_of(0);
             const bool half = A.weight == WEIGHT_LOAD_HALF;
             float2 pa[NPP], pb[NPP];
             sfor<NPP>([&](auto qq) {
@@ -433,13 +469,13 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     }
                 }
             });
-            group_sync<S>(bar_id);
+            if (Wo == WA) group_sync<S>(bar_id);
             sfor<NPP>([&](auto qq) {
                 constexpr int q = decltype(qq)::value;
                 const int k = tid + q * S::NTHR;
                 if (k == 0) {
                     const float x0 = pa[q].x, xl = pb[q].x;  // Im of DC/Nyquist ignored
-                    W[0] = make_float2(x0 + xl, -(x0 - xl));
+                    Wo[0] = make_float2(x0 + xl, -(x0 - xl));
                 } else if (k <= (L >> 1)) {
                     float2 a = pa[q], b = pb[q];
                     if (half) {
@@ -450,17 +486,30 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     const float2 bc = cconj(b);
                     const float2 e = cadd(a, bc);
                     const float2 o = cmulc(csub(a, bc), w);
-                    W[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
-                    if (L - k != k) W[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
+                    Wo[cpad<S>(k)] = cconj(make_float2(e.x - o.y, e.y + o.x));
+                    if (L - k != k) Wo[cpad<S>(L - k)] = cconj(make_float2(e.x + o.y, -e.y + o.x));
                 }
             });
             group_sync<S>(bar_id);
+            cur = Wo;
             from_slot = false;
+            if (pp && ++stage == K) refill();
         }
-        codelet_pass<S, 0, FC2R>(c, W, v, tw, A.ip.pass[0].tw_off, from_slot, last_global, bar_id, post);
-        sfor<S::NP - 1>([&](auto pp) {
-            constexpr int P = decltype(pp)::value + 1;
-            codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off, false, last_global, bar_id);
+        sfor<S::NP>([&](auto pidx) {
+            constexpr int P = decltype(pidx)::value;
+            const bool global_last = P == S::NP - 1 && last_global;
+            float2* Wo = global_last ? WA : out_of(stage);
+            // a barrier between loads and stores: in place (the output is the
+            // input, or overlaps the slot's raw row), or after the loads of a
+            // last pass that reads the slot, before the slot is refilled
+            const bool sync_loaded = global_last ? (from_slot || cur == WA) : (from_slot ? Wo == WA : cur == Wo);
+            codelet_pass<S, P, FC2R && P == 0>(c, cur, Wo, v, tw, A.ip.pass[P].tw_off, from_slot, last_global,
+                                                sync_loaded, bar_id, post);
+            from_slot = false;
+            if (!global_last) {
+                cur = Wo;
+                if (pp && ++stage == K) refill();
+            }
         });
         if (A.io_mode == IO_R2C_EVEN) {
             // post-process pairs:
@@ -475,8 +524,10 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             constexpr int NPO = (L / 2 + 1 + S::NTHR - 1) / S::NTHR;  // pairs per thread
             // pairs are handled in chunks of PCH (all of them when few), every
             // pair of a chunk read before any is stored; the reads only touch
-            // W and the stores only global memory, so chunks need no barrier
+            // shared memory and the stores only global memory, so chunks need
+            // no barrier
             constexpr int PCH = NPO <= 8 ? NPO : 4;
+            const float2* Z = cur;
             sfor<(NPO + PCH - 1) / PCH>([&](auto cc) {
                 constexpr int q0 = decltype(cc)::value * PCH;
                 float2 za[PCH], zb[PCH], wk[PCH];
@@ -484,8 +535,8 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     constexpr int q = q0 + decltype(qq)::value;
                     const int k = tid + q * S::NTHR;
                     if (q < NPO && k <= (L >> 1)) {
-                        za[q - q0] = W[cpad<S>(k)];
-                        zb[q - q0] = W[cpad<S>(L - k)];  // k = 0: entry L, unused
+                        za[q - q0] = Z[cpad<S>(k)];
+                        zb[q - q0] = Z[cpad<S>(L - k)];  // k = 0: entry L, unused
                         wk[q - q0] = post[k];
                     }
                 });
@@ -507,16 +558,12 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                     }
                 });
             });
-            group_sync<S>(bar_id);
+            // the slot is read here when there is no work buffer: all reads
+            // precede its refill (a work buffer is protected by the barrier
+            // at the next transform's start)
+            if (!refilled) group_sync<S>(bar_id);
         }
-        // the slot is free: refill it with the transform NST iterations ahead
-        if (leader) {
-            const int64_t nt = gfirst + (it + NST) * gstride;
-            if (nt < A.ntf) {
-                fence_proxy_async_smem();
-                issue(s, nt);
-            }
-        }
+        if (!refilled) refill();
     }
 }
 
@@ -600,7 +647,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) coltile_kernel(const __grid_
         if (g < TF) {
             sfor<S::NP>([&](auto pp) {
                 constexpr int P = decltype(pp)::value;
-                codelet_pass<S, P>(c, W, v, tw, A.ip.pass[P].tw_off, false, false, bar_id);
+                codelet_pass<S, P>(c, W, W, v, tw, A.ip.pass[P].tw_off, false, false, true, bar_id);
             });
         }
         __syncthreads();

@@ -1,9 +1,13 @@
 // codelet_list.h - the compile-time specialised row kernels that are built.
 // X(id, MAXT, MINB, L, NTHR, radices...): launch bound of MAXT threads per CTA
 // with MINB CTAs per SM (register cap 65536 / (MAXT * MINB)).  The first
-// entry of a length is the spill-free build with the higher register cap,
-// measured faster than the 80-register builds kept as variants (up to 1.2x
-// for 1024-4096 points, whose 80-register builds spill), and for 128/256
+// entry of a length is its fastest spill-free build: for 512-4096 points
+// the higher register cap (the 80-register builds of 1024-4096 spill and
+// ran up to 1.2x slower; the spill-free 80-register 512-point build is 3-6 %
+// faster alone but made the R2C/C2R round trip over N=3000 and N=1024, whose
+// two chains run concurrently, 6 % slower); for 1500 points the lower one
+// (96 registers, 4 CTAs per SM: R2C N=3000 batch 4096 6 % faster than 108
+// registers at 3 CTAs per SM, the round trip 5 % faster); for 128/256
 // points the radix order that keeps all 32 lanes of the transform's warp
 // busy (8*8*4: 1.17x, 4*4*8: 1.11x over 16*16 and 8*16); the planner
 // picks the first entry whose length matches exactly, or the k-th one with
@@ -14,7 +18,7 @@
 // runs in parallel.
 #pragma once
 #define GFFT_CODELETS(X)                       \
-    X(0, 160, 3, 1500, 160, 15, 10, 10)        \
+    X(0, 160, 4, 1500, 160, 15, 10, 10)        \
     X(1, 256, 2, 512, 64, 8, 8, 8)             \
     X(2, 256, 2, 4096, 256, 16, 16, 16)        \
     X(3, 256, 2, 2048, 128, 16, 16, 8)         \
@@ -34,5 +38,7 @@
     X(17, 384, 2, 128, 32, 8, 16)              \
     X(18, 256, 1, 1500, 32, 15, 10, 10)        \
     X(19, 256, 1, 1500, 32, 10, 10, 15)        \
-    X(20, 256, 1, 1500, 64, 15, 10, 10)
-#define GFFT_NUM_CODELETS 21
+    X(20, 256, 1, 1500, 64, 15, 10, 10)        \
+    X(21, 160, 3, 1500, 160, 15, 10, 10)       \
+    X(22, 256, 3, 512, 64, 8, 8, 8)
+#define GFFT_NUM_CODELETS 23

@@ -40,7 +40,7 @@ const char* cache_path()
     return (p && *p) ? p : nullptr;
 }
 
-// file lines: "<key> <variant> <ng> <nst> <codelets> <cluster> <cluster_c>"
+// file lines: "<key> <variant> <ng> <nst> <codelets> <cluster> <cluster_c> <pp>"
 void load_file()
 {
     if (g_file_loaded) return;
@@ -54,12 +54,13 @@ void load_file()
         std::string key;
         PlanHints h;
         if (!(is >> key >> h.codelet_variant >> h.codelet_ng >> h.codelet_nst >> h.codelets >> h.cluster >>
-              h.cluster_c))
+              h.cluster_c >> h.codelet_pp))
             continue;
         if (h.codelet_variant < -1 || h.codelet_variant > 64 || h.codelet_ng < 0 || h.codelet_ng > 15 ||
             h.codelet_nst < 0 || h.codelet_nst > 4 || h.codelets < -1 || h.codelets > 1 || h.cluster < -1 ||
             h.cluster > 1 || (h.cluster_c != 0 && h.cluster_c != 2 && h.cluster_c != 4 && h.cluster_c != 8 &&
-                              h.cluster_c != 16))
+                              h.cluster_c != 16) ||
+            h.codelet_pp < -1 || h.codelet_pp > 1)
             continue;
         g_cache[key] = h;
     }
@@ -73,7 +74,7 @@ void save_file()
     for (const auto& kv : g_cache) {
         const PlanHints& h = kv.second;
         f << kv.first << ' ' << h.codelet_variant << ' ' << h.codelet_ng << ' ' << h.codelet_nst << ' ' << h.codelets
-          << ' ' << h.cluster << ' ' << h.cluster_c << '\n';
+          << ' ' << h.cluster << ' ' << h.cluster_c << ' ' << h.codelet_pp << '\n';
     }
 }
 
@@ -106,7 +107,8 @@ std::string signature(const StepList& sl)
         os << (int)s.kind << '/';
         switch (s.kind) {
         case Step::ROW:
-            os << s.row.codelet << ',' << s.row.ngroups << ',' << s.row.nstage << ',' << s.row.tfpc << ',';
+            os << s.row.codelet << ',' << s.row.ngroups << ',' << s.row.nstage << ',' << s.row.nbuf << ','
+               << s.row.tfpc << ',';
             for (int p = 0; p < s.row.ip.npass; ++p) os << s.row.ip.pass[p].radix << '.';
             break;
         case Step::COL:
@@ -122,7 +124,7 @@ std::string signature(const StepList& sl)
 }
 
 // The candidate choices: the planner's own, every other specialised build
-// of the length, other group/stage shapes of the codelet, cluster sizes,
+// of the length, other group/stage/work-buffer shapes of the codelet, cluster sizes,
 // clusters forced on or off, and no codelets at all.
 std::vector<PlanHints> candidates()
 {
@@ -133,13 +135,15 @@ std::vector<PlanHints> candidates()
         h.codelet_variant = v;
         c.push_back(h);
     }
-    for (int nst : {2, 3})
-        for (int ng : {1, 2, 4, 8}) {
-            PlanHints h;
-            h.codelet_ng = ng;
-            h.codelet_nst = nst;
-            c.push_back(h);
-        }
+    for (int pp : {0, 1})
+        for (int nst : {2, 3})
+            for (int ng : {1, 2, 4, 8}) {
+                PlanHints h;
+                h.codelet_ng = ng;
+                h.codelet_nst = nst;
+                h.codelet_pp = pp;
+                c.push_back(h);
+            }
     for (int cc : {4, 8, 16}) {
         PlanHints h;
         h.cluster_c = cc;

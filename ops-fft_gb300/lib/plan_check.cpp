@@ -85,7 +85,7 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
             return fail(why, "codelet mismatch");
         for (int p = 0; p < cnr; ++p)
             if (cr[p] != a.ip.pass[p].radix) return fail(why, "codelet radix mismatch");
-        if (a.nbuf != 1) return fail(why, "codelet buffers");
+        if (a.nbuf != 1 && a.nbuf != 2) return fail(why, "codelet buffers");
         bool need_tw = false;
         for (int p = 0; p < a.ip.npass; ++p) need_tw |= a.ip.pass[p].ns > 1;
         if (need_tw && a.tw_cnt == 0) return fail(why, "codelet twiddles not in shared memory");
@@ -98,7 +98,11 @@ bool check_row(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
     const int64_t row_bytes = a.in_dist * a.in_esize;
     if ((int64_t)a.tfpc * row_bytes > a.stage_bytes || a.stage_bytes % 16) return fail(why, "row stage too small");
     if (a.codelet >= 0) {
-        const int64_t slots_end = 64 + (int64_t)a.nstage * a.stage_bytes;
+        int64_t slots_end = 64 + (int64_t)a.nstage * a.stage_bytes;
+        if (a.nbuf == 2) {  // work buffer after the slots, 16-byte aligned, lpad float2
+            if (a.smem_work < slots_end || a.smem_work % 16) return fail(why, "codelet work buffer");
+            slots_end = a.smem_work + (int64_t)a.lpad * 8;
+        }
         if (a.stage_bytes < a.in_dist * a.in_esize + 32 || a.stage_bytes < 16 + (int64_t)a.lpad * 8 || a.tfpc != 1)
             return fail(why, "codelet slot too small");
         int cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;

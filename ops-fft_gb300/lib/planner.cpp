@@ -213,6 +213,10 @@ bool clusters_enabled()
 
 namespace {
 
+// Score bonus of a codelet configuration with a per-group work buffer
+// (ping-pong passes) over the in-place one.
+constexpr double kPingPongScore = 0.0;
+
 // Codelet row step (see csrc/codelet.cuh for the execution model and the
 // shared-memory layout).  Returns false when no codelet applies.
 bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, int io_mode, int nreal, int weight,
@@ -267,7 +271,7 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     const int64_t stage_bytes = align(std::max<int64_t>(row_bytes + 32, 16 + (int64_t)lpad * 8), 128);
     const int64_t cta_fixed = align(hdr + tw_bytes + post_bytes, 128);
     const int64_t nslots = (ntf + tps - 1) / tps;
-    double best = -1;
+    double best = -1e300;  // any configuration that fits beats none
     int best_ng = 0, best_ns = 0;
     int64_t best_gb = 0;
     // OPS_FFT_CODELET_NG / OPS_FFT_CODELET_NST pin the groups per CTA and
@@ -276,9 +280,17 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     const char* env_ns = std::getenv("OPS_FFT_CODELET_NST");
     const int force_ng = (t_hints && t_hints->codelet_ng > 0) ? t_hints->codelet_ng : (env_ng ? std::atoi(env_ng) : 0);
     const int force_ns = (t_hints && t_hints->codelet_nst > 0) ? t_hints->codelet_nst : (env_ns ? std::atoi(env_ns) : 0);
+    // a per-group work buffer (ping-pong passes, half the group barriers):
+    // OPS_FFT_CODELET_PP=0/1 or the autotuner pin it; unset, the score decides
+    const char* env_pp = std::getenv("OPS_FFT_CODELET_PP");
+    const int force_pp = (t_hints && t_hints->codelet_pp >= 0) ? t_hints->codelet_pp : (env_pp ? std::atoi(env_pp) : -1);
+    const int64_t work_bytes = align((int64_t)lpad * 8, 128);
+    int best_pp = 0;
+    for (int pp = 0; pp <= 1; ++pp)
     for (int nst = 2; nst <= 4; ++nst) {
+        if (force_pp >= 0 && pp != force_pp) continue;
         if (force_ns ? nst != force_ns : nst > 3) continue;
-        const int64_t gb = align(64 + nst * stage_bytes, 128);
+        const int64_t gb = align(64 + nst * stage_bytes + (pp ? work_bytes : 0), 128);
         for (int ng = 1; ng <= 15 && ng * cn <= cmaxt; ++ng) {
             if (force_ng && ng != force_ng) continue;
             const int64_t smem = cta_fixed + ng * gb;
@@ -296,9 +308,13 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
             // a small batch cannot keep every group busy
             groups_sm = std::min<int64_t>(groups_sm, std::max<int64_t>(1, (nslots + 151) / 152));
             const double occ = (double)std::min<int64_t>(groups_sm * cn, 1536) / 1536.0;
+            // bytes of input copies in flight per SM, saturating at 40 KB
+            // (more stages beyond that measured slower: R2C, C2R and the
+            // weighted R2C adjoint at N=3000, batch 4096, 4 groups per SM,
+            // 2 stages 1-3 % faster than 3)
             const double infl =
-                (double)std::min<int64_t>(groups_sm * (nst - 1) * tps * row_bytes, 64 * 1024) / (64 * 1024.0);
-            const double score = occ + infl - 0.02 * nst;
+                (double)std::min<int64_t>(groups_sm * (nst - 1) * tps * row_bytes, 40 * 1024) / (40 * 1024.0);
+            const double score = occ + infl - 0.02 * nst + kPingPongScore * pp;
             // ties: more groups per CTA (up to 384 threads) share the CTA's
             // twiddle tables and hide each other's barriers (measured faster)
             const bool tie_better = score > best - 1e-9 && ng > best_ng && ng * cn <= 384;
@@ -307,10 +323,11 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
                 best_ng = ng;
                 best_ns = nst;
                 best_gb = gb;
+                best_pp = pp;
             }
         }
     }
-    if (best < 0) return false;
+    if (best_ng == 0) return false;
     tb = trial;
     st.post_off = post_off;
     a.ntf = ntf;
@@ -318,7 +335,7 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     a.out_dist = out_dist;
     a.tfpc = tps;
     a.lpad = lpad;
-    a.nbuf = 1;
+    a.nbuf = best_pp ? 2 : 1;
     a.io_mode = io_mode;
     a.weight = weight;
     a.nreal = nreal;
@@ -335,7 +352,7 @@ bool make_codelet_step(int L, int64_t ntf, int64_t in_dist, int64_t out_dist, in
     a.smem_tw = (int32_t)hdr;
     a.smem_post = (int32_t)(hdr + tw_bytes);
     a.smem_stage = (int32_t)cta_fixed;
-    a.smem_work = 0;
+    a.smem_work = best_pp ? (int32_t)(64 + best_ns * stage_bytes) : 0;  // group offset of the work buffer
     a.group_bytes = (int32_t)best_gb;
     a.ngroups = best_ng;
     a.smem_bytes = (int32_t)(cta_fixed + best_ng * best_gb);

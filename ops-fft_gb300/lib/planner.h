@@ -89,13 +89,15 @@ struct PlanHints {
     int codelet_variant = -1;  // k-th specialised build of the length
     int codelet_ng = 0;        // transform groups per CTA of a codelet
     int codelet_nst = 0;       // input prefetch stages of a codelet
+    int codelet_pp = -1;       // 1: per-group work buffer (ping-pong passes), 0: in place
     int codelets = -1;         // 0: no specialised row kernels
     int cluster = -1;          // 0: no cluster kernels; 1: clusters wherever a configuration exists
     int cluster_c = 0;         // cluster size
     bool operator==(const PlanHints& o) const
     {
         return codelet_variant == o.codelet_variant && codelet_ng == o.codelet_ng && codelet_nst == o.codelet_nst &&
-               codelets == o.codelets && cluster == o.cluster && cluster_c == o.cluster_c;
+               codelet_pp == o.codelet_pp && codelets == o.codelets && cluster == o.cluster &&
+               cluster_c == o.cluster_c;
     }
 };
 
