@@ -250,6 +250,13 @@ ACLFFT_API aclfftResult aclfftDebugSetExecError(aclfftHandle plan, int flags);
  * Process-wide. */
 ACLFFT_API aclfftResult aclfftDebugFailAllocations(int after);
 
+/* Test hook: the in-register butterfly of radix R (1 <= R <= 48) that the
+ * kernels use, evaluated on the host (the same operation sequence and
+ * rounding as the device's paired FP32 instructions): in and out hold R
+ * interleaved complex values (forward DFT, natural order).  Returns
+ * ACLFFT_INVALID_SIZE for other R. */
+ACLFFT_API aclfftResult aclfftDebugButterfly(int R, const float* in, float* out);
+
 /* Human-readable reason of the last failure on this thread ("" if none). */
 ACLFFT_API const char* aclfftGetLastErrorDetail(void);
 

@@ -163,6 +163,7 @@ _SIGNATURES = {
     "aclfftGetExecError": [_H, ctypes.POINTER(_I)],
     "aclfftDebugSetExecError": [_H, _I],
     "aclfftDebugFailAllocations": [_I],
+    "aclfftDebugButterfly": [_I, ctypes.c_void_p, ctypes.c_void_p],
     "aclfftDebugGetTwiddleSegments": [_H, _VP, _I, ctypes.POINTER(_I)],
 }
 

@@ -12,8 +12,14 @@
 //   odd primes p (11..47)  symmetric-pair form: for k = 1..(p-1)/2,
 //                          X_k, X_{p-k} = x0 + sum_j c_jk A_j -/+ i sum_j s_jk B_j
 //                          with A_j = x_j + x_{p-j}, B_j = x_j - x_{p-j}
-//   composite R = A*B      one decimation-in-time split (A-point over B-point)
-//                          with constant inter-stage twiddles W_R^{a*k1}
+//   composite R = A*B      with gcd(A, B) = 1 (6, 10, 12, 14, 15, 18, 20, ...):
+//                          the prime-factor (Good-Thomas) split, no
+//                          inter-stage twiddles: x[(B*n1 + A*n2) mod R]
+//                          through B-point then A-point DFTs, bin k1, k2
+//                          stored at the k with k = k1 mod A, k = k2 mod B;
+//                          otherwise (8, 9, 16, ...) one decimation-in-time
+//                          split (A-point over B-point) with constant
+//                          inter-stage twiddles W_R^{a*k1}
 #pragma once
 #include <cuda_runtime.h>
 #include <type_traits>
@@ -215,6 +221,20 @@ __host__ __device__ constexpr bool is_prime(int n)
         if (n % f == 0) return false;
     return true;
 }
+__host__ __device__ constexpr int gcd_c(int a, int b) { return b == 0 ? a : gcd_c(b, a % b); }
+// x with (a * x) % m == 1 (a, m coprime, m >= 2); 0 for m == 1
+__host__ __device__ constexpr int inv_mod(int a, int m)
+{
+    for (int x = 1; x < m; ++x)
+        if ((a * x) % m == 1) return x;
+    return 0;
+}
+// composite radices whose smallest-factor split is coprime take the
+// prime-factor form
+__host__ __device__ constexpr bool pfa_split(int R)
+{
+    return R > 4 && !is_prime(R) && gcd_c(smallest_factor(R), R / smallest_factor(R)) == 1;
+}
 
 template <int R, class Enable = void>
 struct DFT;
@@ -296,9 +316,49 @@ struct DFT<P, std::enable_if_t<(P >= 5) && is_prime(P)>> {
     }
 };
 
-// Composite radices: R = A * B, decimation in time.
+// Composite radices R = A * B with gcd(A, B) = 1: prime-factor split.
 template <int R>
-struct DFT<R, std::enable_if_t<(R > 4) && !is_prime(R)>> {
+struct DFT<R, std::enable_if_t<pfa_split(R)>> {
+    static constexpr int A = smallest_factor(R);
+    static constexpr int B = R / A;
+    static constexpr int IA = inv_mod(B % A, A);  // B^-1 mod A
+    static constexpr int IB = inv_mod(A % B, B);  // A^-1 mod B
+    GFFT_HD static void run(float2* v)
+    {
+        float2 t[R];
+        sfor<A>([&](auto aa) {
+            constexpr int n1 = decltype(aa)::value;
+            float2 u[B];
+            sfor<B>([&](auto mm) {
+                constexpr int n2 = decltype(mm)::value;
+                u[n2] = v[(B * n1 + A * n2) % R];
+            });
+            DFT<B>::run(u);
+            sfor<B>([&](auto kk) {
+                constexpr int k2 = decltype(kk)::value;
+                t[n1 * B + k2] = u[k2];
+            });
+        });
+        sfor<B>([&](auto kk) {
+            constexpr int k2 = decltype(kk)::value;
+            float2 w[A];
+            sfor<A>([&](auto aa) {
+                constexpr int n1 = decltype(aa)::value;
+                w[n1] = t[n1 * B + k2];
+            });
+            DFT<A>::run(w);
+            sfor<A>([&](auto qq) {
+                constexpr int k1 = decltype(qq)::value;
+                // k = k1 (mod A), k = k2 (mod B)
+                v[(B * ((IA * k1) % A) + A * ((IB * k2) % B)) % R] = w[k1];
+            });
+        });
+    }
+};
+
+// Other composite radices: R = A * B, decimation in time.
+template <int R>
+struct DFT<R, std::enable_if_t<(R > 4) && !is_prime(R) && !pfa_split(R)>> {
     static constexpr int A = smallest_factor(R);
     static constexpr int B = R / A;
     GFFT_HD static void run(float2* v)

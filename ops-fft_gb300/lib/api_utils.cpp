@@ -10,7 +10,10 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <math.h>
+#include <utility>
 
+#include "../csrc/butterfly.cuh"
 #include "handle.h"
 
 namespace gfft {
@@ -42,6 +45,30 @@ bool log_enabled()
 }
 
 }  // namespace gfft
+
+namespace {
+
+template <int R>
+void butterfly_host(const float* in, float* out)
+{
+    float2 v[R];
+    for (int i = 0; i < R; ++i) v[i] = make_float2(in[2 * i], in[2 * i + 1]);
+    gfft::DFT<R>::run(v);
+    for (int i = 0; i < R; ++i) {
+        out[2 * i] = v[i].x;
+        out[2 * i + 1] = v[i].y;
+    }
+}
+
+template <int... Rs>
+bool butterfly_dispatch(int R, const float* in, float* out, std::integer_sequence<int, Rs...>)
+{
+    bool done = false;
+    ((R == Rs + 1 ? (butterfly_host<Rs + 1>(in, out), done = true) : false), ...);
+    return done;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -211,6 +238,16 @@ ACLFFT_API aclfftResult aclfftDebugGetTwiddleSegments(aclfftHandle plan, long lo
         segs[5 * i + 4] = v[i].kind;
     }
     return ACLFFT_SUCCESS;
+}
+
+
+ACLFFT_API aclfftResult aclfftDebugButterfly(int R, const float* in, float* out)
+{
+    ACLFFT_CHECK_NULL(in);
+    ACLFFT_CHECK_NULL(out);
+    ACLFFT_CHECK_PARAM(R >= 1 && R <= 48, ACLFFT_INVALID_SIZE);
+    return butterfly_dispatch(R, in, out, std::make_integer_sequence<int, 48>{}) ? ACLFFT_SUCCESS
+                                                                                 : ACLFFT_INVALID_SIZE;
 }
 
 ACLFFT_API aclfftResult aclfftGetTwiddles(aclfftHandle plan, aclfftComplex* host, long long maxEntries,

@@ -517,3 +517,23 @@ def test_codelet_variants_and_cluster_choices_stay_in_bounds(variant, monkeypatc
     monkeypatch.setenv("OPS_FFT_COLTILE_VARIANT", variant)
     with A.Plan.plan2d(3, 2048, 2048, A.C2C) as p:
         assert p.check() == "ok"
+
+
+def test_butterflies_match_fp64_dft():
+    """Every in-register butterfly the kernels use (radix 1-48: hand-derived
+    small radices, symmetric-pair odd primes, prime-factor splits of coprime
+    composites such as 6, 10, 12, 15 and decimation-in-time splits such as 8,
+    9, 16), evaluated on the host with the device's rounding, against an FP64
+    DFT: relative error within a few FP32 ulps times log R."""
+    mine = A.lib()
+    rng = np.random.default_rng(48)
+    for R in range(1, 49):
+        x = (rng.standard_normal(R) + 1j * rng.standard_normal(R)).astype(np.complex64)
+        out = np.empty(R, dtype=np.complex64)
+        assert mine.aclfftDebugButterfly(R, x.ctypes.data, out.ctypes.data) == A.SUCCESS, R
+        ref = np.fft.fft(x.astype(np.complex128))
+        err = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+        assert err < 2e-7 * max(1.0, np.log2(R)) * 2, (R, err)
+    buf = np.zeros(4, dtype=np.complex64)
+    assert mine.aclfftDebugButterfly(0, buf.ctypes.data, buf.ctypes.data) == A.INVALID_SIZE
+    assert mine.aclfftDebugButterfly(49, buf.ctypes.data, buf.ctypes.data) == A.INVALID_SIZE
