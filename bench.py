@@ -52,8 +52,8 @@ FALLBACK_HBM_GBS = 6800.0
 # Writes of a launch mostly stay in L2 when the kernel ends, so this is below
 # the algorithmic read+write bytes.
 NCU_TRAFFIC = {
-    ("cfg2", "dominant"): 52756480,  # R2C N=3000 batch=4096: 49.21 MB read + 3.54 MB written
-    ("cfg1", "dominant"): None,      # C2C 4096 x 256 now runs on the row codelet: not captured yet
+    ("cfg2", "dominant"): 53330432,  # R2C N=3000 batch=4096: 49.22 MB read + 4.11 MB written
+    ("cfg1", "dominant"): 8472064,   # C2C 4096 x 256 (row codelet): 8.47 MB read, the 8.4 MB output left in L2
     ("cfg3", "dominant"): 68792064,  # TF32x3 N=65536 x 64, both passes: 67.19 MB read + 1.60 MB written
     ("cfg4", "dominant"): 970750000,  # 2D forward: row pass 268.5 + 214.7 MB, column-tile pass 268.5 + 219.0 MB
     ("long", "dominant"): 487250944,  # C2C 65536 x 512 on 16-CTA clusters: 268.73 MB read + 218.52 MB written
