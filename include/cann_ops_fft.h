@@ -131,7 +131,10 @@ ACLFFT_API aclfftResult aclfftExecC2C(aclfftHandle plan, aclfftComplex* idata, a
 ACLFFT_API aclfftResult aclfftExecR2C(aclfftHandle plan, aclfftReal* idata, aclfftComplex* odata);
 ACLFFT_API aclfftResult aclfftExecC2R(aclfftHandle plan, aclfftComplex* idata, aclfftReal* odata);
 
-/* Double precision: not implemented (lib/fft_exec_api.cpp:87-116). */
+/* Double precision (stubs in the reference, lib/fft_exec_api.cpp:87-116):
+ * Z2Z of rank 1-3 (HORIZONTAL or VERTICAL in 1D), D2Z/Z2D of rank 1, same
+ * argument checks, layouts and pointer semantics as the FP32 entries, with
+ * FP64 arithmetic and FP64 twiddles throughout. */
 ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleComplex* odata,
                                       int direction);
 ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata);

@@ -288,6 +288,15 @@ class Plan:
     def exec_c2r(self, x, y) -> None:
         _check(lib().aclfftExecC2R(self.handle, ptr(x), ptr(y)), "aclfftExecC2R")
 
+    def exec_z2z(self, x, y, direction: int = FORWARD) -> None:
+        _check(lib().aclfftExecZ2Z(self.handle, ptr(x), ptr(y), direction), "aclfftExecZ2Z")
+
+    def exec_d2z(self, x, y) -> None:
+        _check(lib().aclfftExecD2Z(self.handle, ptr(x), ptr(y)), "aclfftExecD2Z")
+
+    def exec_z2d(self, x, y) -> None:
+        _check(lib().aclfftExecZ2D(self.handle, ptr(x), ptr(y)), "aclfftExecZ2D")
+
     def exec_c2c_adjoint(self, g_out, g_in, direction: int = FORWARD) -> None:
         _check(lib().aclfftExecC2CAdjoint(self.handle, ptr(g_out), ptr(g_in), direction), "aclfftExecC2CAdjoint")
 

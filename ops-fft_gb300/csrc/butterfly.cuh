@@ -180,29 +180,66 @@ GFFT_HD float2 sum_scale(float2 a, float2 b, float h) { return cscale(cadd(a, b)
 GFFT_HD float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // * (-i)
 GFFT_HD float2 mul_pi(float2 a) { return make_float2(-a.y, a.x); }  // * (+i)
 
-// x * W_R^E with the trivial angles folded at compile time.
-template <int R, int E>
-GFFT_HD float2 twc(float2 x)
+// FP64 complex helpers (double-precision transforms): scalar double ops,
+// fused where the FP32 forms are.
+GFFT_HD double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+GFFT_HD double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+GFFT_HD double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+GFFT_HD double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+GFFT_HD double2 cmul(double2 a, double2 b)
 {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+GFFT_HD double2 cmulc(double2 a, double2 b)
+{
+    return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+GFFT_HD double2 sfma(double s, double2 a, double2 acc) { return make_double2(fma(s, a.x, acc.x), fma(s, a.y, acc.y)); }
+GFFT_HD double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+GFFT_HD double2 sum_scale(double2 a, double2 b, double h) { return cscale(cadd(a, b), h); }
+GFFT_HD double2 mul_mi(double2 a) { return make_double2(a.y, -a.x); }
+GFFT_HD double2 mul_pi(double2 a) { return make_double2(-a.y, a.x); }
+
+// Component type and constructor of a complex vector type.
+template <class C>
+struct CT;
+template <>
+struct CT<float2> {
+    using S = float;
+    GFFT_HD static float2 make(float a, float b) { return make_float2(a, b); }
+};
+template <>
+struct CT<double2> {
+    using S = double;
+    GFFT_HD static double2 make(double a, double b) { return make_double2(a, b); }
+};
+
+// x * W_R^E with the trivial angles folded at compile time.
+template <int R, int E, class C>
+GFFT_HD C twc(C x)
+{
+    using T = CT<C>;
+    using S = typename T::S;
     constexpr int e = ((E % R) + R) % R;
+    constexpr S h = S(W<8, 1>::r.c);  // cos(pi/4)
     if constexpr (e == 0) {
         return x;
     } else if constexpr (2 * e == R) {
-        return make_float2(-x.x, -x.y);
+        return T::make(-x.x, -x.y);
     } else if constexpr (4 * e == R) {
         return mul_mi(x);
     } else if constexpr (4 * e == 3 * R) {
         return mul_pi(x);
     } else if constexpr (8 * e == R) {
-        return sum_scale(make_float2(x.x, x.y), make_float2(x.y, -x.x), W<8, 1>::re);
+        return sum_scale(T::make(x.x, x.y), T::make(x.y, -x.x), h);
     } else if constexpr (8 * e == 3 * R) {
-        return sum_scale(make_float2(x.y, -x.x), make_float2(-x.x, -x.y), W<8, 1>::re);
+        return sum_scale(T::make(x.y, -x.x), T::make(-x.x, -x.y), h);
     } else if constexpr (8 * e == 5 * R) {
-        return sum_scale(make_float2(-x.x, x.x), make_float2(-x.y, -x.y), W<8, 1>::re);
+        return sum_scale(T::make(-x.x, x.x), T::make(-x.y, -x.y), h);
     } else if constexpr (8 * e == 7 * R) {
-        return sum_scale(make_float2(x.x, x.x), make_float2(-x.y, x.y), W<8, 1>::re);
+        return sum_scale(T::make(x.x, x.x), T::make(-x.y, x.y), h);
     } else {
-        return cmul(x, make_float2(W<R, e>::re, W<R, e>::im));
+        return cmul(x, T::make(S(W<R, e>::r.c), S(-W<R, e>::r.s)));
     }
 }
 
@@ -236,19 +273,24 @@ __host__ __device__ constexpr bool pfa_split(int R)
     return R > 4 && !is_prime(R) && gcd_c(smallest_factor(R), R / smallest_factor(R)) == 1;
 }
 
+// DFT<R>::run(v) on float2 (FP32 kernels) or double2 (FP64 transforms).
 template <int R, class Enable = void>
 struct DFT;
 
 template <>
 struct DFT<1> {
-    GFFT_HD static void run(float2*) {}
+    template <class C>
+    GFFT_HD static void run(C*)
+    {
+    }
 };
 
 template <>
 struct DFT<2> {
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
-        const float2 a = v[0], b = v[1];
+        const C a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
     }
@@ -256,13 +298,16 @@ struct DFT<2> {
 
 template <>
 struct DFT<3> {
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
-        constexpr float s3 = float(0.86602540378443864676372317075294);  // sin(2pi/3)
-        const float2 t1 = cadd(v[1], v[2]);
-        const float2 t2 = sfma(-0.5f, t1, v[0]);
-        const float2 d = csub(v[1], v[2]);
-        const float2 t3 = pmul(make_float2(s3, -s3), make_float2(d.y, d.x));  // -i*s3*(v1-v2)
+        using T = CT<C>;
+        using S = typename T::S;
+        constexpr S s3 = S(0.86602540378443864676372317075294);  // sin(2pi/3)
+        const C t1 = cadd(v[1], v[2]);
+        const C t2 = sfma(S(-0.5), t1, v[0]);
+        const C d = csub(v[1], v[2]);
+        const C t3 = pmul(T::make(s3, -s3), T::make(d.y, d.x));  // -i*s3*(v1-v2)
         v[0] = cadd(v[0], t1);
         v[1] = cadd(t2, t3);
         v[2] = csub(t2, t3);
@@ -271,10 +316,11 @@ struct DFT<3> {
 
 template <>
 struct DFT<4> {
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
-        const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-        const float2 c = cadd(v[1], v[3]), d = mul_mi(csub(v[1], v[3]));
+        const C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        const C c = cadd(v[1], v[3]), d = mul_mi(csub(v[1], v[3]));
         v[0] = cadd(a, c);
         v[2] = csub(a, c);
         v[1] = cadd(b, d);
@@ -285,33 +331,36 @@ struct DFT<4> {
 // Odd primes >= 5: symmetric-pair evaluation.
 template <int P>
 struct DFT<P, std::enable_if_t<(P >= 5) && is_prime(P)>> {
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
+        using T = CT<C>;
+        using S = typename T::S;
         constexpr int H = (P - 1) / 2;
-        float2 A[H], B[H];
-        float2 sum = v[0];
+        C A[H], B[H];
+        C sum = v[0];
         sfor<H>([&](auto jj) {
             constexpr int j = decltype(jj)::value + 1;
             A[j - 1] = cadd(v[j], v[P - j]);
             B[j - 1] = csub(v[j], v[P - j]);
             sum = cadd(sum, A[j - 1]);
         });
-        const float2 x0 = v[0];
+        const C x0 = v[0];
         v[0] = sum;
         sfor<H>([&](auto kk) {
             constexpr int k = decltype(kk)::value + 1;
-            float2 re = x0;                       // x0 + sum c*A
-            float2 im = make_float2(0.f, 0.f);    // sum s*B
+            C re = x0;                       // x0 + sum c*A
+            C im = T::make(S(0), S(0));      // sum s*B
             sfor<H>([&](auto jj) {
                 constexpr int j = decltype(jj)::value + 1;
                 constexpr Root rt = unit_root((long long)j * k, P);
-                constexpr float c = float(rt.c), s = float(rt.s);
+                constexpr S c = S(rt.c), s = S(rt.s);
                 re = sfma(c, A[j - 1], re);
                 im = sfma(s, B[j - 1], im);
             });
             // X_k = re - i*im ; X_{P-k} = re + i*im
-            v[k] = cadd(re, make_float2(im.y, -im.x));
-            v[P - k] = cadd(re, make_float2(-im.y, im.x));
+            v[k] = cadd(re, T::make(im.y, -im.x));
+            v[P - k] = cadd(re, T::make(-im.y, im.x));
         });
     }
 };
@@ -323,12 +372,13 @@ struct DFT<R, std::enable_if_t<pfa_split(R)>> {
     static constexpr int B = R / A;
     static constexpr int IA = inv_mod(B % A, A);  // B^-1 mod A
     static constexpr int IB = inv_mod(A % B, B);  // A^-1 mod B
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
-        float2 t[R];
+        C t[R];
         sfor<A>([&](auto aa) {
             constexpr int n1 = decltype(aa)::value;
-            float2 u[B];
+            C u[B];
             sfor<B>([&](auto mm) {
                 constexpr int n2 = decltype(mm)::value;
                 u[n2] = v[(B * n1 + A * n2) % R];
@@ -341,7 +391,7 @@ struct DFT<R, std::enable_if_t<pfa_split(R)>> {
         });
         sfor<B>([&](auto kk) {
             constexpr int k2 = decltype(kk)::value;
-            float2 w[A];
+            C w[A];
             sfor<A>([&](auto aa) {
                 constexpr int n1 = decltype(aa)::value;
                 w[n1] = t[n1 * B + k2];
@@ -361,12 +411,13 @@ template <int R>
 struct DFT<R, std::enable_if_t<(R > 4) && !is_prime(R) && !pfa_split(R)>> {
     static constexpr int A = smallest_factor(R);
     static constexpr int B = R / A;
-    GFFT_HD static void run(float2* v)
+    template <class C>
+    GFFT_HD static void run(C* v)
     {
-        float2 t[R];
+        C t[R];
         sfor<A>([&](auto aa) {
             constexpr int a = decltype(aa)::value;
-            float2 u[B];
+            C u[B];
             sfor<B>([&](auto mm) {
                 constexpr int m = decltype(mm)::value;
                 u[m] = v[a + A * m];
@@ -379,7 +430,7 @@ struct DFT<R, std::enable_if_t<(R > 4) && !is_prime(R) && !pfa_split(R)>> {
         });
         sfor<B>([&](auto kk) {
             constexpr int k1 = decltype(kk)::value;
-            float2 w[A];
+            C w[A];
             sfor<A>([&](auto aa) {
                 constexpr int a = decltype(aa)::value;
                 w[a] = t[a * B + k1];

@@ -300,7 +300,48 @@ struct TwSeg {
 }  // namespace gfft
 
 // Launchers exported by the CUDA translation units (C linkage, plain types).
+namespace gfft {
+
+// Double-precision transforms: one radix-R Stockham pass, global memory to
+// global memory.  Transform t (0 <= t < ntf) has element i at
+//   base(t) + i*stride,  base(t) = (t / split)*hi + (t % split)*lo
+// (double2 units; double units for a real input or output).  Butterfly j of
+// the pass reads elements j + r*(n/R), multiplies them by W_{ns*R}^{(j%ns)*r}
+// (read from the table W_n^m, m < n, at m = (j%ns)*r*n/(ns*R)), runs the
+// R-point DFT and writes element (j/ns)*ns*R + j%ns + r*ns.
+enum DIo : int32_t {
+    DIO_C2C = 0,       // complex in, complex out
+    DIO_REAL_IN = 1,   // first pass of a D2Z: real input, imaginary parts zero
+    DIO_HERM_IN = 2,   // first pass of a Z2D: bins 0..n/2 of a Hermitian
+                       // spectrum, expanded and conjugated (the backward
+                       // transform as a forward one)
+    DIO_HALF_OUT = 4,  // last pass of a D2Z: bins 0..n/2 only
+    DIO_REAL_OUT = 8,  // last pass of a Z2D: real parts only
+};
+struct DPassArgs {
+    const void* in;
+    void* out;
+    const void* tw;  // double2 W_n^m, m < n
+    int64_t ntf;
+    int64_t in_split, in_hi, in_lo, in_stride;
+    int64_t out_split, out_hi, out_lo, out_stride;
+    int32_t n;
+    int32_t radix;
+    int32_t ns;
+    int32_t io;        // DIo bits
+    int32_t conj_in;   // conjugate on load (backward C2C)
+    int32_t conj_out;  // conjugate on store
+    int32_t t_fast;    // 1: consecutive threads take consecutive transforms (strided axes)
+    int32_t pad_;
+    double scale;
+};
+
+}  // namespace gfft
+
 extern "C" {
+int gfft_launch_dpass(const gfft::DPassArgs* a, void* stream);
+// Fills table[m] = exp(-2 pi i m / n) in FP64 for m < n.
+int gfft_gen_dtwiddles(void* table, long long n, void* stream);
 int gfft_launch_row(const gfft::RowArgs* a, void* stream);
 int gfft_launch_col(const gfft::ColArgs* a, void* stream);
 int gfft_launch_pack(const gfft::PackArgs* a, void* stream);

@@ -79,26 +79,32 @@ double points(const aclfftHandle_t* h)
     return n;
 }
 
-float norm_scale(const aclfftHandle_t* h, bool backward_like)
+// The plan's output scale (FP32 kernels take it rounded to float).
+double norm_scale(const aclfftHandle_t* h, bool backward_like)
 {
     const double n = points(h);
     switch (h->normMode) {
-    case ACLFFT_NORM_BACKWARD: return backward_like ? (float)(1.0 / n) : 1.f;
-    case ACLFFT_NORM_ORTHO: return (float)(1.0 / std::sqrt(n));
-    case ACLFFT_NORM_FORWARD: return backward_like ? 1.f : (float)(1.0 / n);
-    default: return 1.f;
+    case ACLFFT_NORM_BACKWARD: return backward_like ? 1.0 / n : 1.0;
+    case ACLFFT_NORM_ORTHO: return 1.0 / std::sqrt(n);
+    case ACLFFT_NORM_FORWARD: return backward_like ? 1.0 : 1.0 / n;
+    default: return 1.0;
     }
 }
 
 int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStream_t st, bool c2c, bool inverse,
-                float scale, const float* wload = nullptr)
+                double dscale, const float* wload = nullptr)
 {
     void* bufs[4] = {in, out, impl->ws, impl->ws2};
     const float2* tw = static_cast<const float2*>(impl->tw);
+    const float scale = (float)dscale;
     const size_t n = sl.steps.size();
+    // the first and last computing steps (copies move data only)
+    size_t i_first = 0, i_last = n ? n - 1 : 0;
+    while (i_first + 1 < n && sl.steps[i_first].kind == Step::COPY) ++i_first;
+    while (i_last > 0 && sl.steps[i_last].kind == Step::COPY) --i_last;
     for (size_t i = 0; i < n; ++i) {
         Step s = sl.steps[i];
-        const bool first = i == 0, last = i + 1 == n;
+        const bool first = i == i_first, last = i == i_last;
         void* src = bufs[s.src];
         void* dst = bufs[s.dst];
         int rc = 0;
@@ -142,6 +148,17 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
             break;
         case Step::COPY:
             rc = (int)cudaMemcpyAsync(dst, src, (size_t)s.copy_bytes, cudaMemcpyDeviceToDevice, st);
+            break;
+        case Step::DPASS:
+            s.dp.in = src;
+            s.dp.out = dst;
+            s.dp.tw = tw + s.dtw_off;
+            if (c2c) {
+                s.dp.conj_in = first && inverse;
+                s.dp.conj_out = last && inverse;
+            }
+            if (last) s.dp.scale = dscale;
+            rc = gfft_launch_dpass(&s.dp, st);
             break;
         case Step::TC:
             s.tc.in = src;
@@ -315,7 +332,7 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
         gfft::set_last_error("plan executed on a different device than it was created on");
         return ACLFFT_INVALID_DEVICE;
     }
-    const float scale = norm_scale(h, backward_like);
+    const double scale = norm_scale(h, backward_like);
     cudaStream_t st = h->stream;
     const Mem min = classify(in, dev), mout = classify(out, dev);
     if (min == Mem::FOREIGN || mout == Mem::FOREIGN) {
@@ -350,7 +367,7 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     void* dev_out = dout ? out : impl->stage_b;
     if (!din && !dout && primary.steps.size() == 1 && primary.steps[0].kind == Step::ROW) {
         const int rc = exec_host_pipelined(impl, primary.steps[0], in, out, shape.in_bytes, shape.out_bytes, st, c2c,
-                                           inverse, scale);
+                                           inverse, (float)scale);
         if (rc > 0) return ACLFFT_EXEC_FAILED;
         if (rc == 0) return drain_error_word(impl, st, nullptr);
     }
@@ -497,7 +514,7 @@ ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const ac
         gfft::set_last_error("weighted adjoint: device pointers of the plan's device only");
         return ACLFFT_INVALID_VALUE;
     }
-    const float scale = norm_scale(plan, false);
+    const double scale = norm_scale(plan, false);
     return launch_list(impl, sl, const_cast<aclfftComplex*>(gradOut), gradIn, plan->stream, false, false, scale,
                        weights) == 0
                ? ACLFFT_SUCCESS
@@ -512,30 +529,32 @@ ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* grad
                        true);
 }
 
+// Double precision (the reference declares these and returns
+// ACLFFT_NOT_IMPLEMENTED, lib/fft_exec_api.cpp:87-116): the same checks and
+// pointer semantics as the single-precision entries.
 ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleComplex* odata,
                                       int direction)
 {
-    (void)plan;
-    (void)idata;
-    (void)odata;
-    (void)direction;
-    return ACLFFT_NOT_IMPLEMENTED;
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_Z2Z);
+    ACLFFT_CHECK_PARAM(direction == ACLFFT_FORWARD || direction == ACLFFT_BACKWARD, ACLFFT_INVALID_VALUE);
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
+    const size_t bytes = complex_elems(plan) * 16;
+    const bool inv = direction == ACLFFT_BACKWARD;
+    return exec_common(plan, 0, idata, odata, {bytes, bytes}, true, inv, inv);
 }
 
 ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata)
 {
-    (void)plan;
-    (void)idata;
-    (void)odata;
-    return ACLFFT_NOT_IMPLEMENTED;
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_D2Z);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 0, idata, odata, {real_elems(plan) * 8, half_elems(plan) * 16}, false, false, false);
 }
 
 ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleReal* odata)
 {
-    (void)plan;
-    (void)idata;
-    (void)odata;
-    return ACLFFT_NOT_IMPLEMENTED;
+    EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_Z2D);
+    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    return exec_common(plan, 0, idata, odata, {half_elems(plan) * 16, real_elems(plan) * 8}, false, false, true);
 }
 
 ACLFFT_API aclfftResult aclfftGetExecError(aclfftHandle plan, int* flags)

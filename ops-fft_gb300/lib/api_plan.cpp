@@ -19,8 +19,8 @@
 // R2C/C2R (the reference rejects them until its 2D real path lands,
 // lib/fft_plan_init_api.cpp:200-209), and 3D plans exist for C2C (the
 // reference's MakePlan3d returns ACLFFT_NOT_IMPLEMENTED, :250-254).  Double
-// precision (Z2Z/D2Z/Z2D) is rejected at plan time at every rank, as in the
-// reference's 1D and 2D entries.
+// precision is planned too (the reference rejects it at plan time,
+// lib/fft_plan_init_api.cpp:132-136): Z2Z at every rank, D2Z/Z2D in 1D.
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -103,13 +103,16 @@ PlanImpl* plan_steps(const aclfftHandle_t* h, aclfftResult* why)
     }
     Problem pr;
     pr.rank = h->rank;
-    pr.kind = h->type == ACLFFT_C2C ? Kind::C2C : (h->type == ACLFFT_R2C ? Kind::R2C : Kind::C2R);
+    pr.dbl = h->type == ACLFFT_Z2Z || h->type == ACLFFT_D2Z || h->type == ACLFFT_Z2D;
+    pr.kind = (h->type == ACLFFT_C2C || h->type == ACLFFT_Z2Z)
+                  ? Kind::C2C
+                  : ((h->type == ACLFFT_R2C || h->type == ACLFFT_D2Z) ? Kind::R2C : Kind::C2R);
     pr.n0 = h->lengths[0];
     pr.n1 = h->rank >= 2 ? h->lengths[1] : 1;
     pr.n2 = h->rank == 3 ? h->lengths[2] : 1;
     pr.batch = h->batch;
     pr.stride = h->rank == 1 ? h->stride[0] : 1;
-    pr.prec = pr.kind == Kind::C2C && pr.rank == 1 ? h->precision : 0;
+    pr.prec = pr.kind == Kind::C2C && pr.rank == 1 && !pr.dbl ? h->precision : 0;
     pr.hints = h->hints;
     impl->prob = pr;
     impl->auto_ws = h->auto_allocate;
@@ -314,8 +317,12 @@ aclfftResult plan_device_setup(PlanImpl* p)
         set_last_error("cudaMalloc of the error word failed");
         return ACLFFT_ALLOC_FAILED;
     }
-    if (!p->tb.segs.empty()) {
-        const int rc = gfft_gen_twiddles(p->tw, p->tb.segs.data(), (int)p->tb.segs.size(), nullptr);
+    if (!p->tb.segs.empty() || !p->tb.dsegs.empty()) {
+        int rc = p->tb.segs.empty() ? 0 : gfft_gen_twiddles(p->tw, p->tb.segs.data(), (int)p->tb.segs.size(), nullptr);
+        for (const auto& d : p->tb.dsegs) {
+            if (rc != 0) break;
+            rc = gfft_gen_dtwiddles(static_cast<float2*>(p->tw) + d.first, d.second, nullptr);
+        }
         if (rc != 0 || cudaStreamSynchronize(nullptr) != cudaSuccess) {
             cudaGetLastError();
             plan_impl_free(p);
@@ -369,10 +376,6 @@ ACLFFT_API aclfftResult aclfftMakePlan1d(aclfftHandle plan, int nx, aclfftType t
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(dimType == ACLFFT_HORIZONTAL || dimType == ACLFFT_VERTICAL, ACLFFT_INVALID_VALUE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
-        GFFT_LOG("aclfftMakePlan1d: type=%d has no 1D execution implementation yet", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     if (validate_1d_size(dimType, nx, "aclfftMakePlan1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
     plan->rank = 1;
     plan->lengths[0] = nx;
@@ -401,7 +404,7 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) {
         GFFT_LOG("aclfftMakePlan2d: type=%d has no 2D execution implementation yet", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -431,7 +434,7 @@ ACLFFT_API aclfftResult aclfftMakePlan3d(aclfftHandle plan, int nx, int ny, int 
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) {
+    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) {
         GFFT_LOG("aclfftMakePlan3d: type=%d has no 3D execution implementation", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -457,10 +460,6 @@ ACLFFT_API aclfftResult aclfftPlan1d(aclfftHandle* plan, int nx, aclfftType type
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(dimType == ACLFFT_HORIZONTAL || dimType == ACLFFT_VERTICAL, ACLFFT_INVALID_VALUE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
-        GFFT_LOG("aclfftPlan1d: type=%d has no 1D execution implementation yet", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     if (validate_1d_size(dimType, nx, "aclfftPlan1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
     aclfftResult r = aclfftCreate(plan);
     if (r != ACLFFT_SUCCESS) return r;
@@ -479,7 +478,7 @@ ACLFFT_API aclfftResult aclfftPlan2d(aclfftHandle* plan, int batch, int nx, int 
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) {
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) {
         GFFT_LOG("aclfftPlan2d: type=%d has no 2D execution implementation yet", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -500,7 +499,7 @@ ACLFFT_API aclfftResult aclfftPlan3d(aclfftHandle* plan, int nx, int ny, int nz,
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) {
+    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) {
         GFFT_LOG("aclfftPlan3d: type=%d has no 3D execution implementation", (int)type);
         return ACLFFT_NOT_SUPPORTED;
     }
@@ -532,7 +531,6 @@ ACLFFT_API aclfftResult aclfftGetSize1d(aclfftHandle plan, int nx, aclfftType ty
     ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) return ACLFFT_NOT_SUPPORTED;
     if (validate_1d_size(ACLFFT_HORIZONTAL, nx, "aclfftGetSize1d") != ACLFFT_SUCCESS) return ACLFFT_INVALID_SIZE;
     aclfftHandle_t d;
     d.rank = 1;
@@ -552,7 +550,7 @@ ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclff
     ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R) return ACLFFT_NOT_SUPPORTED;
+    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) return ACLFFT_NOT_SUPPORTED;
     aclfftHandle_t d;
     d.rank = 2;
     d.lengths[0] = nx;
@@ -573,7 +571,7 @@ ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int n
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C) return ACLFFT_NOT_SUPPORTED;
+    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) return ACLFFT_NOT_SUPPORTED;
     aclfftHandle_t d;
     d.rank = 3;
     d.lengths[0] = nx;

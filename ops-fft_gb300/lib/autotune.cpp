@@ -203,8 +203,9 @@ aclfftResult autotune_plan(aclfftHandle_t* h)
     if (!cur->device_ready) {
         if (plan_device_setup(cur) != ACLFFT_SUCCESS || !cur->device_ready) return ACLFFT_EXEC_FAILED;
     }
-    // split-precision forms have fixed launches; VERTICAL plans one column kernel
-    if (h->precision != 0 || (h->rank == 1 && h->stride[0] > 1) || !cur->lists[0].supported) {
+    // split-precision forms have fixed launches; VERTICAL plans one column
+    // kernel; double precision one pass kernel per radix
+    if (h->precision != 0 || (h->rank == 1 && h->stride[0] > 1) || !cur->lists[0].supported || cur->prob.dbl) {
         h->tuned = 0;
         h->tune_candidates = 0;
         return ACLFFT_SUCCESS;

@@ -283,6 +283,31 @@ bool check_tc(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
 // Cluster transform: the configuration matches the length, every HBM
 // access of the column loads and row stores, the twiddle ranges and the
 // receive-buffer offsets of the distributed shared-memory stores.
+// Double-precision pass: radix and stage consistent, table inside the blob,
+// every element read and written inside its buffer.
+bool check_dpass(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
+{
+    const DPassArgs& a = s.dp;
+    if (a.n < 1 || a.radix < 1 || a.radix > 47 || a.n % a.radix || a.ns < 1 || (a.n / a.radix) % a.ns)
+        return fail(why, "dpass radix");
+    if (a.ntf < 1 || a.in_split < 1 || a.out_split < 1 || a.in_stride < 1 || a.out_stride < 1)
+        return fail(why, "dpass layout");
+    if (s.dtw_off < 0 || s.dtw_off % 2 || s.dtw_off + 2 * (int64_t)a.n > tw_count) return fail(why, "dpass table");
+    auto max_base = [&](int64_t split, int64_t hi, int64_t lo) {
+        return ((a.ntf - 1) / split) * hi + std::min<int64_t>(split - 1, a.ntf - 1) * lo;
+    };
+    const bool herm = (a.io & DIO_HERM_IN) != 0, real_in = (a.io & DIO_REAL_IN) != 0;
+    const bool half = (a.io & DIO_HALF_OUT) != 0, real_out = (a.io & DIO_REAL_OUT) != 0;
+    const int64_t in_last = herm ? a.n / 2 : a.n - 1, out_last = half ? a.n / 2 : a.n - 1;
+    const int64_t in_need = (max_base(a.in_split, a.in_hi, a.in_lo) + in_last * a.in_stride + 1) * (real_in ? 8 : 16);
+    const int64_t out_need =
+        (max_base(a.out_split, a.out_hi, a.out_lo) + out_last * a.out_stride + 1) * (real_out ? 8 : 16);
+    if (in_need > b.bytes[s.src]) return fail(why, "dpass input out of bounds");
+    if (out_need > b.bytes[s.dst]) return fail(why, "dpass output out of bounds");
+    if (s.src == s.dst) return fail(why, "dpass in place");
+    return true;
+}
+
 bool check_cluster(const Step& s, const Bufs& b, int64_t tw_count, std::string& why)
 {
     const ClusterArgs& a = s.cl;
@@ -357,9 +382,10 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
         outer *= p.n0 * p.n1;
         last = p.n2;
     }
-    const int64_t cbytes = p.rank == 1 ? p.batch * p.n0 * std::max<int64_t>(p.stride, 1) * 8 : outer * last * 8;
-    const int64_t rbytes = outer * last * 4;
-    const int64_t hbytes = outer * (last / 2 + 1) * 8;
+    const int64_t es = p.dbl ? 2 : 1;  // double precision: twice the bytes per element
+    const int64_t cbytes = (p.rank == 1 ? p.batch * p.n0 * std::max<int64_t>(p.stride, 1) * 8 : outer * last * 8) * es;
+    const int64_t rbytes = outer * last * 4 * es;
+    const int64_t hbytes = outer * (last / 2 + 1) * 8 * es;
     for (int v = 0; v < 4; ++v) {
         const StepList& sl = impl->lists[v];
         if (!sl.supported) continue;
@@ -388,6 +414,7 @@ extern "C" ACLFFT_API int aclfftDebugCheckPlan(aclfftHandle plan, char* msg, int
             else if (s.kind == Step::PACK) ok = check_pack(s, b, impl->tb.count, why);
             else if (s.kind == Step::TC) ok = check_tc(s, b, impl->tb.count, why);
             else if (s.kind == Step::CLUSTER) ok = check_cluster(s, b, impl->tb.count, why);
+            else if (s.kind == Step::DPASS) ok = check_dpass(s, b, impl->tb.count, why);
             else if (s.kind == Step::COPY)
                 ok = (s.copy_bytes <= b.bytes[s.src] && s.copy_bytes <= b.bytes[s.dst]) || fail(why, "copy size");
             if (!ok) {

@@ -136,6 +136,16 @@ int64_t TwiddleBuilder::add_dft_matrix(int R, int prec)
     return off;
 }
 
+int64_t TwiddleBuilder::add_dtable(int64_t n)
+{
+    for (const auto& d : dsegs)
+        if (d.second == n) return d.first;
+    const int64_t off = count;
+    dsegs.emplace_back(off, n);
+    count += 2 * n;
+    return off;
+}
+
 bool build_inner(int L, const std::vector<int>& radices, int nthr, TwiddleBuilder& tb, InnerPlan& ip)
 {
     if (radices.empty() || (int)radices.size() > kMaxPass) return false;
@@ -842,9 +852,158 @@ bool build_tc_c2c_steps(int64_t n, int64_t batch, int prec, bool inplace, Twiddl
     return true;
 }
 
+namespace {
+
+// Element addressing of one side of a double-precision pass (see DPassArgs).
+struct DLayout {
+    int64_t split = 1, hi = 0, lo = 0, stride = 1;
+};
+
+// Double precision: every axis as global-memory Stockham passes
+// (csrc/dfft.cu).  A pass never writes the buffer it reads: the passes of an
+// axis go src -> WS / WS2 (alternating) -> ... -> OUT, one launch per radix.
+bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
+                  int64_t& ws2_bytes)
+{
+    auto unsupported = [&](const char* why) {
+        out.supported = false;
+        out.why = why;
+        return true;
+    };
+    if (p.weight != WEIGHT_NONE) return unsupported("double precision has no adjoint entries");
+    const int IN = inplace ? BUF_OUT : BUF_IN;
+    int cur = IN;
+    // one axis: ntf transforms of length n; `src` / `dst` the layouts of the
+    // first pass's input and the last pass's output, `mid` the layout of the
+    // intermediates; io bits of the first and the last pass
+    auto axis = [&](int64_t n, int64_t ntf, DLayout src, DLayout mid, DLayout dst, int io_first, int io_last,
+                    bool t_fast) -> bool {
+        const std::vector<int> rad = choose_radices((int)n);
+        if (rad.empty()) return false;
+        const int k = (int)rad.size();
+        const int64_t toff = tb.add_dtable(n);
+        int from = cur;
+        int next_ws = (from == BUF_WS) ? BUF_WS2 : BUF_WS;
+        int64_t ns = 1;
+        for (int i = 0; i < k; ++i) {
+            const bool last = i + 1 == k;
+            int to = last ? BUF_OUT : next_ws;
+            if (last && from == BUF_OUT) to = next_ws;  // a one-pass axis on the output: via a workspace
+            Step st;
+            st.kind = Step::DPASS;
+            DPassArgs& a = st.dp;
+            a.ntf = ntf;
+            a.n = (int32_t)n;
+            a.radix = rad[i];
+            a.ns = (int32_t)ns;
+            a.io = (i == 0 ? io_first : 0) | (last ? io_last : 0);
+            a.t_fast = t_fast ? 1 : 0;
+            a.scale = 1.0;
+            const DLayout& li = i == 0 ? src : mid;
+            const DLayout& lo = (last && to == BUF_OUT) ? dst : mid;
+            a.in_split = li.split;
+            a.in_hi = li.hi;
+            a.in_lo = li.lo;
+            a.in_stride = li.stride;
+            a.out_split = lo.split;
+            a.out_hi = lo.hi;
+            a.out_lo = lo.lo;
+            a.out_stride = lo.stride;
+            st.dtw_off = toff;
+            st.src = from;
+            st.dst = to;
+            out.steps.push_back(st);
+            if (to != BUF_OUT) next_ws = (to == BUF_WS) ? BUF_WS2 : BUF_WS;
+            from = to;
+            ns *= rad[i];
+        }
+        if (from != BUF_OUT) {  // the axis ended in a workspace laid out like the output
+            Step cp;
+            cp.kind = Step::COPY;
+            cp.src = from;
+            cp.dst = BUF_OUT;
+            out.steps.push_back(cp);
+        }
+        cur = BUF_OUT;
+        return true;
+    };
+
+    if (p.kind == Kind::C2C) {
+        const int nd = p.rank;
+        const int64_t dims[3] = {p.n0, nd >= 2 ? p.n1 : 1, nd == 3 ? p.n2 : 1};
+        int64_t total = p.batch * std::max<int64_t>(p.stride, 1);
+        for (int a = 0; a < nd; ++a) total *= dims[a];
+        for (int a = 0; a < nd; ++a)
+            if (!length_supported(dims[a])) return unsupported("length has a prime factor > 47");
+        for (int a = nd - 1; a >= 0; --a) {
+            const int64_t n = dims[a];
+            int64_t S = (nd == 1) ? std::max<int64_t>(p.stride, 1) : 1;
+            for (int b = a + 1; b < nd; ++b) S *= dims[b];
+            if (n == 1) continue;
+            DLayout l;
+            l.split = S;
+            l.hi = n * S;
+            l.lo = 1;
+            l.stride = S;
+            if (!axis(n, total / n, l, l, l, 0, 0, S > 1)) return unsupported("length not decomposable");
+        }
+        if (out.steps.empty() && IN != BUF_OUT) {
+            Step cp;
+            cp.kind = Step::COPY;
+            cp.src = IN;
+            cp.dst = BUF_OUT;
+            out.steps.push_back(cp);
+        }
+        for (Step& s : out.steps)
+            if (s.kind == Step::COPY) s.copy_bytes = total * 16;
+        ws_bytes = ws2_bytes = total * 16;
+        return true;
+    }
+    if (p.rank != 1 || p.stride > 1) return unsupported("double-precision real transforms are 1D, horizontal");
+    const int64_t n = p.n0, nb = n / 2 + 1;
+    if (!length_supported(n)) return unsupported("length has a prime factor > 47");
+    const bool d2z = p.kind == Kind::R2C;
+    const int64_t in_bytes = d2z ? p.batch * n * 8 : p.batch * nb * 16;
+    if (inplace) {
+        // input and output rows have different pitches: the input moves to
+        // the second workspace first
+        Step cp;
+        cp.kind = Step::COPY;
+        cp.copy_bytes = in_bytes;
+        cp.src = BUF_OUT;
+        cp.dst = BUF_WS2;
+        out.steps.push_back(cp);
+        cur = BUF_WS2;
+    }
+    DLayout full, half, real;
+    full.hi = n;
+    half.hi = nb;
+    real.hi = n;
+    if (!axis(n, p.batch, d2z ? real : half, full, d2z ? half : real, d2z ? DIO_REAL_IN : DIO_HERM_IN,
+              d2z ? DIO_HALF_OUT : DIO_REAL_OUT, false))
+        return unsupported("length not decomposable");
+    // (the axis starts from the input or its copy in WS2, never from the
+    // output, so its last pass writes the output directly: a copy could not
+    // change the row pitch)
+    for (const Step& s : out.steps)
+        if (s.kind == Step::COPY && s.dst == BUF_OUT) return false;
+    ws_bytes = p.batch * n * 16;
+    ws2_bytes = std::max<int64_t>(p.batch * n * 16, in_bytes);
+    return true;
+}
+
+}  // namespace
+
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
                  int64_t& ws2_bytes)
 {
+    if (p.dbl) {
+        const HintScope hints(&p.hints);
+        out = StepList{};
+        ws_bytes = 0;
+        ws2_bytes = 0;
+        return build_dsteps(p, inplace, tb, out, ws_bytes, ws2_bytes);
+    }
     const HintScope hints(&p.hints);
     out = StepList{};
     ws_bytes = 0;

@@ -12,6 +12,7 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../csrc/kernel_args.h"
@@ -42,19 +43,21 @@ std::vector<int> split_axis(int64_t n, int cap);
 enum BufId : int { BUF_IN = 0, BUF_OUT = 1, BUF_WS = 2, BUF_WS2 = 3 };
 
 struct Step {
-    enum Kind { ROW, COL, PACK, COPY, TC, CLUSTER } kind = ROW;
+    enum Kind { ROW, COL, PACK, COPY, TC, CLUSTER, DPASS } kind = ROW;
     int64_t copy_bytes = 0;
     RowArgs row{};
     ColArgs col{};
     PackArgs pack{};
     TcArgs tc{};
     ClusterArgs cl{};
+    DPassArgs dp{};  // double precision
     int src = BUF_IN;
     int dst = BUF_OUT;
     // Offsets (float2 units) into the plan's twiddle blob for the pointers
     // patched at exec time; -1 when unused.
     int64_t tw_off = -1, post_off = -1, hi_off = -1, lo_off = -1;
     int64_t bmat_off = -1;  // TC: DFT-matrix operand images
+    int64_t dtw_off = -1;   // DPASS: FP64 table W_n^m (float2 units, 2 per entry)
 };
 
 // Everything needed to run one transform kind (forward / adjoint variants
@@ -68,6 +71,10 @@ struct StepList {
 struct TwiddleBuilder {
     std::vector<TwSeg> segs;
     int64_t count = 0;  // float2 entries so far (kept 2-aligned)
+    // FP64 tables W_n^m, m < n (double precision plans): (offset, n), each
+    // 2n float2 entries of the blob
+    std::vector<std::pair<int64_t, int64_t>> dsegs;
+    int64_t add_dtable(int64_t n);
     int64_t add_pass_table(int64_t ns, int R);        // rows of R, W_{ns*R}^{k*r}
     int64_t add_linear(int64_t count, int64_t M, int64_t mult);  // W_M^{i*mult}
     int64_t add_dft_matrix(int R, int prec);  // tensor-core operand images (kind 3)
@@ -110,6 +117,7 @@ struct Problem {
     int64_t stride = 1;      // VERTICAL 1D: stride between samples (= batch), batch = 1
     int weight = WEIGHT_NONE;
     int prec = 0;            // 0: FP32 Stockham; TcPrec: split-precision tensor-core stages (C2C)
+    bool dbl = false;        // double precision (Z2Z / D2Z / Z2D)
 };
 
 bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& out, int64_t& ws_bytes,
