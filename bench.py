@@ -1045,6 +1045,46 @@ def extra_multidim(torch, A, dev, stream, timer, nk, reps, warmup, peak):
     return out
 
 
+def extra_double(torch, A, dev, stream, timer, nk, reps, warmup, peak):
+    """Double precision (Z2Z / D2Z, one exec each on device buffers): time,
+    GB/s of one read plus one write, nominal FP64 GFLOP/s (5 N log2 N per
+    complex transform, half for a real one), and cuFFT (torch.fft on
+    complex128 / float64) on the same shapes for scale."""
+    import math
+
+    g = torch.Generator(device=dev).manual_seed(9)
+    z = torch.complex(torch.randn((2048, 4096), generator=g, device=dev, dtype=torch.float64),
+                      torch.randn((2048, 4096), generator=g, device=dev, dtype=torch.float64))
+    zo = torch.empty_like(z)
+    r = torch.randn((4096, 3000), generator=g, device=dev, dtype=torch.float64)
+    ro = torch.empty((4096, 1501), dtype=torch.complex128, device=dev)
+    cases = [
+        ("Z2Z 4096 x 2048", A.Plan.plan1d(4096, A.Z2Z, 2048), lambda p: p.exec_z2z(z, zo, A.FORWARD),
+         lambda: torch.fft.fft(z, out=zo), 2 * z.numel() * 16, 2048 * 5 * 4096 * math.log2(4096)),
+        ("D2Z 3000 x 4096", A.Plan.plan1d(3000, A.D2Z, 4096), lambda p: p.exec_d2z(r, ro),
+         lambda: torch.fft.rfft(r, out=ro), r.numel() * 8 + ro.numel() * 16, 4096 * 2.5 * 3000 * math.log2(3000)),
+    ]
+    out = {}
+    for name, plan, call, lib, byt, flops in cases:
+        plan.set_stream(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                call(plan)
+                lib()
+        torch.cuda.synchronize()
+        t = timer(lambda i, p=plan, c=call: c(p), nk, reps) or timer.eager(lambda i, p=plan, c=call: c(p), nk, reps)
+        tl = timer(lambda i: lib(), nk, reps) or timer.eager(lambda i: lib(), nk, reps)
+        us = statistics.median(t) / nk * 1e3
+        out[name] = {"us": round(us, 1), "GB/s": round(byt / (us / 1e6) / 1e9, 1),
+                     "frac_of_measured_hbm": round(byt / (us / 1e6) / 1e9 / peak, 3),
+                     "fp64_GFLOP/s_nominal": round(flops / (us / 1e6) / 1e9, 1), "launches": plan.info().nsteps,
+                     "cufft_us": round(statistics.median(tl) / nk * 1e3, 1)}
+        plan.destroy()
+    del z, zo, r, ro
+    torch.cuda.empty_cache()
+    return out
+
+
 def extra_autograd(torch, dev, stream, nk, reps, warmup):
     """The headline step through the torch.autograd wrappers (torch_fft):
     X = rfft(x), y = irfft(X, n), loss = sum(w*|X|^2), loss.backward() -
@@ -1252,6 +1292,8 @@ def main():
                                                               args.warmup, l2, peak)
         extras["autograd_step"] = extra_autograd(torch, dev, stream, nk, max(5, reps // 4), args.warmup)
         extras["multidim_2d_3d"] = extra_multidim(torch, A, dev, stream, timer, nk, max(5, reps // 4), args.warmup,
+                                                  peak)
+        extras["double_precision"] = extra_double(torch, A, dev, stream, timer, nk, max(5, reps // 4), args.warmup,
                                                   peak)
         wl = make_workload(args.workload, torch, A, dev, stream, 1)
 
