@@ -317,6 +317,13 @@ enum DIo : int32_t {
                        // transform as a forward one)
     DIO_HALF_OUT = 4,  // last pass of a D2Z: bins 0..n/2 only
     DIO_REAL_OUT = 8,  // last pass of a Z2D: real parts only
+    // even N (n = 2L): not a pass but the real-data step around an L-point
+    // transform; rows of L complex values (the real row viewed as complex)
+    DIO_R2C_POST = 16,  // Z (L values) -> X (L + 1 bins), even/odd post-process
+    DIO_C2R_PRE = 32,   // X (L + 1 bins) -> conj(Z') (L values), Hermitian pre-process
+    DIO_PAIR_IN = 64,   // complex input read as two doubles (a real row viewed as
+                        // complex: 8-byte alignment suffices)
+    DIO_PAIR_OUT = 128, // complex output written as two doubles
 };
 struct DPassArgs {
     const void* in;

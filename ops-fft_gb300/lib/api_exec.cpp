@@ -303,6 +303,10 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
 struct CallShape {
     size_t in_bytes;
     size_t out_bytes;
+    // alignment the kernels need of device pointers: the complex element
+    // (8 bytes FP32, 16 FP64); real FP64 rows are read as double pairs (8)
+    size_t in_align = 8;
+    size_t out_align = 8;
 };
 
 // variant 0 = primary transform, 2 = adjoint transform
@@ -340,6 +344,11 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
         return ACLFFT_INVALID_VALUE;
     }
     const bool din = min == Mem::DEVICE, dout = mout == Mem::DEVICE;
+    if ((din && reinterpret_cast<uintptr_t>(in) % shape.in_align) ||
+        (dout && reinterpret_cast<uintptr_t>(out) % shape.out_align)) {
+        gfft::set_last_error("a device data pointer is not aligned to the transform's complex element");
+        return ACLFFT_UNALIGNED_DATA;
+    }
     if (din && dout) {
         const StepList& sl = (in == out) ? impl->lists[variant + 1] : primary;
         if (!sl.supported) return ACLFFT_NOT_IMPLEMENTED;
@@ -540,21 +549,23 @@ ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* id
     if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     const size_t bytes = complex_elems(plan) * 16;
     const bool inv = direction == ACLFFT_BACKWARD;
-    return exec_common(plan, 0, idata, odata, {bytes, bytes}, true, inv, inv);
+    return exec_common(plan, 0, idata, odata, {bytes, bytes, 16, 16}, true, inv, inv);
 }
 
 ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_D2Z);
     if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
-    return exec_common(plan, 0, idata, odata, {real_elems(plan) * 8, half_elems(plan) * 16}, false, false, false);
+    return exec_common(plan, 0, idata, odata, {real_elems(plan) * 8, half_elems(plan) * 16, 8, 16}, false, false,
+                       false);
 }
 
 ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleReal* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_Z2D);
     if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
-    return exec_common(plan, 0, idata, odata, {half_elems(plan) * 16, real_elems(plan) * 8}, false, false, true);
+    return exec_common(plan, 0, idata, odata, {half_elems(plan) * 16, real_elems(plan) * 8, 16, 8}, false, false,
+                       true);
 }
 
 ACLFFT_API aclfftResult aclfftGetExecError(aclfftHandle plan, int* flags)

@@ -298,7 +298,16 @@ bool check_dpass(const Step& s, const Bufs& b, int64_t tw_count, std::string& wh
     };
     const bool herm = (a.io & DIO_HERM_IN) != 0, real_in = (a.io & DIO_REAL_IN) != 0;
     const bool half = (a.io & DIO_HALF_OUT) != 0, real_out = (a.io & DIO_REAL_OUT) != 0;
-    const int64_t in_last = herm ? a.n / 2 : a.n - 1, out_last = half ? a.n / 2 : a.n - 1;
+    int64_t in_last = herm ? a.n / 2 : a.n - 1, out_last = half ? a.n / 2 : a.n - 1;
+    if (a.io & (DIO_R2C_POST | DIO_C2R_PRE)) {
+        // the real-data step of an even N = 2L: rows of L values and of L + 1 bins
+        if (a.n % 2 || a.radix != 1 || a.ns != 1 || a.in_split != 1 || a.out_split != 1 || a.in_stride != 1 ||
+            a.out_stride != 1)
+            return fail(why, "dpass real step layout");
+        const bool post = (a.io & DIO_R2C_POST) != 0;
+        in_last = post ? a.n / 2 - 1 : a.n / 2;
+        out_last = post ? a.n / 2 : a.n / 2 - 1;
+    }
     const int64_t in_need = (max_base(a.in_split, a.in_hi, a.in_lo) + in_last * a.in_stride + 1) * (real_in ? 8 : 16);
     const int64_t out_need =
         (max_base(a.out_split, a.out_hi, a.out_lo) + out_last * a.out_stride + 1) * (real_out ? 8 : 16);

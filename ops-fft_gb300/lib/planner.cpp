@@ -876,8 +876,10 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
     // one axis: ntf transforms of length n; `src` / `dst` the layouts of the
     // first pass's input and the last pass's output, `mid` the layout of the
     // intermediates; io bits of the first and the last pass
+    // (in_ws: the last pass writes a workspace instead of the output, for a
+    // step that follows; `cur` then names that workspace)
     auto axis = [&](int64_t n, int64_t ntf, DLayout src, DLayout mid, DLayout dst, int io_first, int io_last,
-                    bool t_fast) -> bool {
+                    bool t_fast, bool in_ws = false) -> bool {
         const std::vector<int> rad = choose_radices((int)n);
         if (rad.empty()) return false;
         const int k = (int)rad.size();
@@ -887,7 +889,7 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
         int64_t ns = 1;
         for (int i = 0; i < k; ++i) {
             const bool last = i + 1 == k;
-            int to = last ? BUF_OUT : next_ws;
+            int to = (last && !in_ws) ? BUF_OUT : next_ws;
             if (last && from == BUF_OUT) to = next_ws;  // a one-pass axis on the output: via a workspace
             Step st;
             st.kind = Step::DPASS;
@@ -916,6 +918,10 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
             if (to != BUF_OUT) next_ws = (to == BUF_WS) ? BUF_WS2 : BUF_WS;
             from = to;
             ns *= rad[i];
+        }
+        if (in_ws) {
+            cur = from;
+            return true;
         }
         if (from != BUF_OUT) {  // the axis ended in a workspace laid out like the output
             Step cp;
@@ -964,6 +970,49 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
     if (!length_supported(n)) return unsupported("length has a prime factor > 47");
     const bool d2z = p.kind == Kind::R2C;
     const int64_t in_bytes = d2z ? p.batch * n * 8 : p.batch * nb * 16;
+    if (n % 2 == 0) {
+        // even N: the real row is an L = N/2 complex row; an L-point
+        // transform and the even/odd post-process (D2Z), or the Hermitian
+        // pre-process and an L-point transform (Z2D), as in the FP32 path
+        const int64_t L = n / 2;
+        DLayout rowL, rowH;
+        rowL.hi = L;
+        rowH.hi = nb;
+        const int64_t toff = tb.add_dtable(n);  // W_N^k for the pre/post-process
+        Step pp;
+        pp.kind = Step::DPASS;
+        DPassArgs& a = pp.dp;
+        a.ntf = p.batch;
+        a.n = (int32_t)n;
+        a.radix = 1;
+        a.ns = 1;
+        a.scale = 1.0;
+        a.in_split = a.out_split = 1;
+        a.in_stride = a.out_stride = 1;
+        pp.dtw_off = toff;
+        if (d2z) {
+            if (!axis(L, p.batch, rowL, rowL, rowL, DIO_PAIR_IN, 0, false, true))
+                return unsupported("length not decomposable");
+            a.io = DIO_R2C_POST;
+            a.in_hi = L;
+            a.out_hi = nb;
+            pp.src = cur;
+            pp.dst = BUF_OUT;
+            out.steps.push_back(pp);
+        } else {
+            a.io = DIO_C2R_PRE;
+            a.in_hi = nb;
+            a.out_hi = L;
+            pp.src = IN;
+            pp.dst = BUF_WS2;
+            out.steps.push_back(pp);
+            cur = BUF_WS2;
+            if (!axis(L, p.batch, rowL, rowL, rowL, 0, DIO_PAIR_OUT, false)) return unsupported("length not decomposable");
+            out.steps.back().dp.conj_out = 1;  // the backward transform as a forward one
+        }
+        ws_bytes = ws2_bytes = p.batch * std::max<int64_t>(L, nb) * 16;
+        return true;
+    }
     if (inplace) {
         // input and output rows have different pitches: the input moves to
         // the second workspace first

@@ -123,3 +123,23 @@ def test_z2z_vertical_and_multidim():
             for d in (A.FORWARD, A.BACKWARD):
                 p.exec_z2z(x, y, d)
                 _ok(y, O.c2c_3d(x, d), ("z2z 3d", dims, d))
+
+
+def test_unaligned_device_pointers_are_rejected():
+    """Device pointers must be aligned to the complex element the kernels
+    load (8 bytes FP32, 16 bytes FP64; real FP64 rows 8): otherwise the exec
+    returns ACLFFT_UNALIGNED_DATA before any launch."""
+    buf = torch.zeros(4096 + 4, dtype=torch.float64, device=_dev())
+    base = buf.data_ptr()
+    lib = A.lib()
+    with A.Plan.plan1d(256, A.Z2Z, 2) as p:
+        assert lib.aclfftExecZ2Z(p.handle, base + 8, base + 4096, A.FORWARD) == A.UNALIGNED_DATA
+        assert lib.aclfftExecZ2Z(p.handle, base, base + 4096 + 8, A.FORWARD) == A.UNALIGNED_DATA
+    with A.Plan.plan1d(256, A.D2Z, 2) as p:
+        # real rows need 8 bytes only; the half spectrum 16
+        assert lib.aclfftExecD2Z(p.handle, base + 8, base + 8192 - 8) == A.UNALIGNED_DATA
+        torch.cuda.synchronize()
+        assert lib.aclfftExecD2Z(p.handle, base + 8, base + 8192) == A.SUCCESS
+        torch.cuda.synchronize()
+    with A.Plan.plan1d(256, A.C2C, 2) as p:
+        assert lib.aclfftExecC2C(p.handle, base + 4, base + 8192, A.FORWARD) == A.UNALIGNED_DATA
