@@ -8,6 +8,9 @@
     y2 = F.irfft2(X2, (nx, ny))
     Z2 = F.fft2(z2); Z3 = F.fftn(z3)   # 2D / 3D C2C over the last axes
 
+complex128 / float64 tensors run in double precision (Z2Z of rank 1-3,
+D2Z / Z2D in 1D); everything else in single precision.
+
 Every forward and backward call is one aclfftExec* / aclfftExec*Adjoint call
 on the current torch stream (3D: one call per leading batch item, the 3D
 plans have no batch).  Plans are cached per (kind, dims, batch, device,
@@ -87,19 +90,38 @@ def _half(dims: tuple) -> tuple:
     return tuple(dims[:-1]) + (dims[-1] // 2 + 1,)
 
 
+def _interior(n: int, value: float, device, dtype) -> torch.Tensor:
+    """Per-bin factor of an n-point real transform's n//2+1 bins: `value` on
+    the interior bins, 1 at DC and (even n) Nyquist."""
+    w = torch.full((n // 2 + 1,), value, dtype=dtype, device=device)
+    w[0] = 1
+    if n % 2 == 0:
+        w[-1] = 1
+    return w
+
+
 class _C2C(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x: torch.Tensor, inverse: bool, nd: int):
         dims = tuple(x.shape[-nd:])
-        x, b = _rows(x.to(torch.complex64), math.prod(dims))
+        dbl = x.dtype == torch.complex128
+        x, b = _rows(x.to(torch.complex128 if dbl else torch.complex64), math.prod(dims))
         y = torch.empty_like(x)
-        _run(A.C2C, dims, b, x.device, "exec_c2c", x, y, A.BACKWARD if inverse else A.FORWARD)
+        _run(A.Z2Z if dbl else A.C2C, dims, b, x.device, "exec_z2z" if dbl else "exec_c2c", x, y,
+             A.BACKWARD if inverse else A.FORWARD)
         ctx.inverse = inverse
         ctx.dims = dims
+        ctx.dbl = dbl
         return y
 
     @staticmethod
     def backward(ctx, g: torch.Tensor):
+        if ctx.dbl:
+            # the adjoint of an unnormalised transform is the opposite-direction one
+            g, b = _rows(g.to(torch.complex128), math.prod(ctx.dims))
+            gx = torch.empty_like(g)
+            _run(A.Z2Z, ctx.dims, b, g.device, "exec_z2z", g, gx, A.FORWARD if ctx.inverse else A.BACKWARD)
+            return gx, None, None
         g, b = _rows(g.to(torch.complex64), math.prod(ctx.dims))
         gx = torch.empty_like(g)
         _run(A.C2C, ctx.dims, b, g.device, "exec_c2c_adjoint", g, gx, A.BACKWARD if ctx.inverse else A.FORWARD)
@@ -110,15 +132,26 @@ class _R2C(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x: torch.Tensor, nd: int):
         dims = tuple(x.shape[-nd:])
-        x, b = _rows(x.to(torch.float32), math.prod(dims))
-        out = torch.empty(x.shape[:-1] + (dims[-1] // 2 + 1,), dtype=torch.complex64, device=x.device)
-        _run(A.R2C, dims, b, x.device, "exec_r2c", x, out)
+        dbl = x.dtype == torch.float64
+        x, b = _rows(x.to(torch.float64 if dbl else torch.float32), math.prod(dims))
+        out = torch.empty(x.shape[:-1] + (dims[-1] // 2 + 1,), dtype=torch.complex128 if dbl else torch.complex64,
+                          device=x.device)
+        _run(A.D2Z if dbl else A.R2C, dims, b, x.device, "exec_d2z" if dbl else "exec_r2c", x, out)
         ctx.dims = dims
+        ctx.dbl = dbl
         return out
 
     @staticmethod
     def backward(ctx, g: torch.Tensor):
         dims = ctx.dims
+        if ctx.dbl:
+            # R2C adjoint: C2R of the gradient with its interior bins halved
+            n = dims[-1]
+            g = g.to(torch.complex128) * _interior(n, 0.5, g.device, torch.float64)
+            g, b = _rows(g, math.prod(_half(dims)))
+            gx = torch.empty(g.shape[:-1] + (n,), dtype=torch.float64, device=g.device)
+            _run(A.Z2D, dims, b, g.device, "exec_z2d", g, gx)
+            return gx, None
         g, b = _rows(g.to(torch.complex64), math.prod(_half(dims)))
         gx = torch.empty(g.shape[:-1] + (dims[-1],), dtype=torch.float32, device=g.device)
         _run(A.R2C, dims, b, g.device, "exec_r2c_adjoint", g, gx)
@@ -130,15 +163,24 @@ class _C2R(torch.autograd.Function):
     def forward(ctx, X: torch.Tensor, dims: tuple):
         if tuple(X.shape[-len(dims):]) != _half(dims):
             raise ValueError(f"C2R to {dims} takes (..., {', '.join(map(str, _half(dims)))}) bins, got {tuple(X.shape)}")
-        X, b = _rows(X.to(torch.complex64), math.prod(_half(dims)))
-        out = torch.empty(X.shape[:-1] + (dims[-1],), dtype=torch.float32, device=X.device)
-        _run(A.C2R, dims, b, X.device, "exec_c2r", X, out)
+        dbl = X.dtype == torch.complex128
+        X, b = _rows(X.to(torch.complex128 if dbl else torch.complex64), math.prod(_half(dims)))
+        out = torch.empty(X.shape[:-1] + (dims[-1],), dtype=torch.float64 if dbl else torch.float32, device=X.device)
+        _run(A.Z2D if dbl else A.C2R, dims, b, X.device, "exec_z2d" if dbl else "exec_c2r", X, out)
         ctx.dims = dims
+        ctx.dbl = dbl
         return out
 
     @staticmethod
     def backward(ctx, g: torch.Tensor):
         dims = ctx.dims
+        if ctx.dbl:
+            # C2R adjoint: R2C of the gradient with its interior bins doubled
+            n = dims[-1]
+            g, b = _rows(g.to(torch.float64), math.prod(dims))
+            gX = torch.empty(g.shape[:-1] + (n // 2 + 1,), dtype=torch.complex128, device=g.device)
+            _run(A.D2Z, dims, b, g.device, "exec_d2z", g, gX)
+            return gX * _interior(n, 2.0, g.device, torch.float64), None
         g, b = _rows(g.to(torch.float32), math.prod(dims))
         gX = torch.empty(g.shape[:-1] + (dims[-1] // 2 + 1,), dtype=torch.complex64, device=g.device)
         _run(A.C2R, dims, b, g.device, "exec_c2r_adjoint", g, gX)

@@ -179,3 +179,38 @@ def test_fft2_fftn_forward_and_gradient(F, inverse):
         torch.real(torch.conj(torch.tensor(G)) * Zt).sum().backward()
         assert _rel(Z.detach().cpu().numpy(), Zt.detach().numpy()) <= REL, shape
         assert _rel(zd.grad.cpu().numpy(), zt.grad.numpy()) <= REL, shape
+
+
+@pytest.mark.parametrize("n", [64, 63])
+def test_double_precision_wrappers_and_gradients(F, n):
+    """complex128 / float64 tensors go through the double-precision entries:
+    values against torch.fft in FP64 at 1e-12, and gradients of real losses
+    through fft, rfft and irfft against torch's FP64 autograd."""
+    rng = np.random.default_rng(n)
+    b = 4
+    z = rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))
+    x = rng.standard_normal((b, n))
+    G = rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))
+    w = rng.uniform(0, 1, (b, n // 2 + 1))
+    v = rng.standard_normal((b, n))
+    zd = torch.tensor(z, device="cuda", requires_grad=True)
+    xd = torch.tensor(x, device="cuda", requires_grad=True)
+    Z = F.fft(zd)
+    X = F.rfft(xd)
+    y = F.irfft(X, n)
+    assert Z.dtype == torch.complex128 and X.dtype == torch.complex128 and y.dtype == torch.float64
+    loss = torch.real(torch.conj(torch.tensor(G, device="cuda")) * Z).sum() + \
+        (torch.tensor(w, device="cuda") * X.abs() ** 2).sum() + (torch.tensor(v, device="cuda") * y).sum()
+    loss.backward()
+    zt = torch.tensor(z, requires_grad=True)
+    xt = torch.tensor(x, requires_grad=True)
+    Zt = torch.fft.fft(zt)
+    Xt = torch.fft.rfft(xt)
+    yt = torch.fft.irfft(Xt, n=n) * n
+    (torch.real(torch.conj(torch.tensor(G)) * Zt).sum() + (torch.tensor(w) * Xt.abs() ** 2).sum() +
+     (torch.tensor(v) * yt).sum()).backward()
+    assert _rel(Z.detach().cpu().numpy(), Zt.detach().numpy()) <= 1e-12
+    assert _rel(X.detach().cpu().numpy(), Xt.detach().numpy()) <= 1e-12
+    assert _rel(y.detach().cpu().numpy(), yt.detach().numpy()) <= 1e-12
+    assert _rel(zd.grad.cpu().numpy(), zt.grad.numpy()) <= 1e-12
+    assert _rel(xd.grad.cpu().numpy(), xt.grad.numpy()) <= 1e-12
