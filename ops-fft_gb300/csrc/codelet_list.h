@@ -13,10 +13,12 @@
 // picks the first entry whose length matches exactly, or the k-th one with
 // OPS_FFT_CODELET_VARIANT=k (entries after the first for a length are
 // variants: other register caps or radix orders; a column pass takes the
-// first entry of its length whose launch bound holds 8 columns: entries 23
-// and 24 exist for that, the 512- and 1024-point column passes of 2D and 3D
-// transforms, measured 15-34 % faster than the column kernel on 512^3,
-// 64 x 1024^2, 8 x 1024^2 and 64 x 512^2).  Each entry is
+// entry of its length whose launch bound holds the most columns, 8 to 16:
+// entries 23-25 exist for that, the 512- and 1024-point column passes of 2D
+// and 3D transforms, measured 15-34 % faster than the column kernel on
+// 512^3, 64 x 1024^2, 8 x 1024^2 and 64 x 512^2, and entry 25's 16 columns
+// of 512 points (32 threads each) another 12 % on 512^3; 16-column builds
+// for 256 and 1024 points were slower or no faster).  Each entry is
 // instantiated in its own translation unit (codelet_<id>.cu) so the build
 // runs in parallel.
 #pragma once
@@ -45,5 +47,6 @@
     X(21, 160, 3, 1500, 160, 15, 10, 10)       \
     X(22, 256, 3, 512, 64, 8, 8, 8)            \
     X(23, 512, 1, 512, 64, 8, 8, 8)            \
-    X(24, 512, 1, 1024, 64, 16, 16, 4)
-#define GFFT_NUM_CODELETS 25
+    X(24, 512, 1, 1024, 64, 16, 16, 4)         \
+    X(25, 512, 1, 512, 32, 8, 8, 8)
+#define GFFT_NUM_CODELETS 26

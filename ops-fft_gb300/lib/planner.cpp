@@ -537,9 +537,12 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     // plain column passes of a length with a codelet run as column tiles of
     // that codelet (one transform group per column, in-place passes)
     if (Ns == 1 && !staged_out && codelets_enabled()) {
-        // the first codelet of this length whose launch bound holds 8 columns
-        // (OPS_FFT_COLTILE_VARIANT=k: the k-th codelet of the length, tiles of
-        // at least 4 columns; tuning experiments)
+        // the codelet of this length whose launch bound holds the most
+        // columns, 8 at least and up to 16 (wider tiles read longer row
+        // segments: 16 columns of 512 points, 128-byte segments, ran the
+        // strided axes of a 512^3 C2C 12 % faster than 8); the first such
+        // entry on ties (OPS_FFT_COLTILE_VARIANT=k: the k-th codelet of the
+        // length, tiles of at least 4 columns; tuning experiments)
         int id = -1, cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
         const char* env_cv = std::getenv("OPS_FFT_COLTILE_VARIANT");
         int min_tf = 8;
@@ -550,10 +553,19 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
                 min_tf = 4;
             }
         }
-        for (int k = 0; id < 0; ++k) {
-            const int cand = gfft_codelet_find(Lq, k);
-            if (cand < 0) break;
-            if (gfft_codelet_info(cand, &cl, &cn, cr, &cnr, &cmaxt, &cminb) == 0 && 8 * cn <= cmaxt) id = cand;
+        if (id < 0) {
+            int best_cols = 0;
+            for (int k = 0;; ++k) {
+                const int cand = gfft_codelet_find(Lq, k);
+                if (cand < 0) break;
+                if (gfft_codelet_info(cand, &cl, &cn, cr, &cnr, &cmaxt, &cminb) != 0) continue;
+                const int cols = std::min(16, cmaxt / cn);
+                if (cols >= 8 && cols > best_cols) {
+                    best_cols = cols;
+                    id = cand;
+                }
+            }
+            if (id >= 0) gfft_codelet_info(id, &cl, &cn, cr, &cnr, &cmaxt, &cminb);
         }
         if (id >= 0) {
             TwiddleBuilder trial = tb;
@@ -571,7 +583,7 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
                 const int pshift = (cr[0] % 2 == 0) ? 4 : 30;
                 const int64_t wsize = ((int64_t)(Lq - 1) + ((int64_t)(Lq - 1) >> pshift) + 1) | 1;
                 int tfc = 1;
-                while (tfc * 2 * cn <= cmaxt && tfc < 8) tfc *= 2;
+                while (tfc * 2 * cn <= cmaxt && tfc < 16) tfc *= 2;
                 const int64_t twb = (tw_cnt * 8 + 127) & ~int64_t(127);
                 // up to 72 KB per CTA (several CTAs per SM) when the launch bound
                 // allows more than one CTA per SM; a single-CTA bound takes all
