@@ -2,7 +2,7 @@
 """Benchmark of the batched FP32 transform path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--reps R] [--impl ours|reference]
-                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5|long] [--no-extras]
+                    [--workload cfg2|cfg1|cfg3|cfg4|cfg5|long|c2c3d|fp64] [--no-extras]
 
 Prints ONE JSON line (rank 0).  Default workload (cfg2): the 1D R2C -> C2R
 round trip with gradients at N = 3000 (2^3*3*5^3) and N = 1024, batch 4096,
@@ -391,6 +391,85 @@ class C2CWorkload:
         return {"workload": self.name, "sizes": [list(s) for s in self.sizes], "dtype": "complex64 interleaved"}
 
 
+class OneExecWorkload:
+    """One forward exec per step of a plan beyond the BASELINE configs, for
+    measurement and profiling: ``c2c3d`` a 3D C2C of 512^3 (z rows, then
+    512-point column tiles along y and x); ``fp64`` a double-precision Z2Z of
+    4096 x 2048 (three FP64 Stockham passes)."""
+
+    def __init__(self, torch, A, dev, stream, nsets, kind):
+        self.torch, self.A, self.kind = torch, A, kind
+        g = torch.Generator(device="cpu").manual_seed(12345)
+        if kind == "c2c3d":
+            self.shape, dt = (512, 512, 512), torch.complex64
+            self.plan = A.Plan.plan3d(512, 512, 512)
+            self.call = "exec_c2c"
+            self.name = "3D C2C 512x512x512 forward"
+        else:
+            self.shape, dt = (2048, 4096), torch.complex128
+            self.plan = A.Plan.plan1d(4096, A.Z2Z, 2048)
+            self.call = "exec_z2z"
+            self.name = "1D Z2Z (FP64) N=4096 batch=2048 forward"
+        self.plan.set_stream(stream)
+        self.sets = []
+        for _ in range(nsets):
+            x = torch.complex(torch.randn(self.shape, generator=g, dtype=dt.to_real()),
+                              torch.randn(self.shape, generator=g, dtype=dt.to_real()))
+            self.sets.append(dict(x=x.to(dev), y=torch.empty(self.shape, dtype=dt, device=dev)))
+        per = 2 * self.sets[0]["x"].numel() * self.sets[0]["x"].element_size()
+        self.alg_bytes_per_step = per
+        self.launches_per_step = self.plan.info().nsteps
+        self.dominant = (self.name, per)
+        self.set_bytes = per
+
+    def _exec(self, s):
+        getattr(self.plan, self.call)(s["x"], s["y"], self.A.FORWARD)
+
+    def step(self, i, dom_events=None):
+        s = self.sets[i % len(self.sets)]
+        if dom_events is not None:
+            dom_events[0].record()
+        self._exec(s)
+        if dom_events is not None:
+            dom_events[1].record()
+
+    def dom_call(self, i):
+        self._exec(self.sets[i % len(self.sets)])
+
+    def make_host(self):
+        torch = self.torch
+        s = self.sets[0]
+        self.host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in s.items()}
+        self.host["x"].copy_(s["x"].cpu())
+        b = self.alg_bytes_per_step // 2
+        return b, b
+
+    def step_host(self):
+        self._exec(self.host)
+
+    def cpu_sample(self, O, rows, nthreads):
+        import numpy as np
+
+        rng = np.random.default_rng(0)
+        t0 = time.perf_counter()
+        if self.kind == "c2c3d":
+            # a 64 x 512 x 512 slab: rows, then the two strided axes
+            x = (rng.standard_normal((64, 512, 512)) + 1j * rng.standard_normal((64, 512, 512))).astype(np.complex64)
+            y = O.port_c2c(x.reshape(-1, 512), -1, nthreads).reshape(x.shape)
+            y = O.port_c2c(np.ascontiguousarray(y.transpose(0, 2, 1)).reshape(-1, 512), -1, nthreads)
+            O.port_c2c(y.reshape(64, 512 * 512).T.copy(), -1, nthreads)
+            return 16 * x.size, time.perf_counter() - t0
+        r = max(1, min(2048, rows))
+        x = rng.standard_normal((r, 4096)) + 1j * rng.standard_normal((r, 4096))
+        O.c2c(x, -1)
+        return 32 * x.size, time.perf_counter() - t0
+
+    def config(self):
+        return {"workload": self.name, "shape": list(self.shape),
+                "dtype": "complex64" if self.kind == "c2c3d" else "complex128",
+                "launches_per_step": self.launches_per_step}
+
+
 class Cfg4:
     """2D C2C 2048 x 2048, batch 8: forward, inverse normalised by 1/(2048^2),
     and the backward pass of L = sum Re(conj(Y) * G) (the adjoint of the
@@ -727,6 +806,8 @@ def make_workload(name, torch, A, dev, stream, nsets):
         return Cfg5(torch, A, dev, stream, nsets)
     if name == "long":
         return LongWorkload(torch, A, dev, stream, nsets)
+    if name in ("c2c3d", "fp64"):
+        return OneExecWorkload(torch, A, dev, stream, nsets, name)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -824,6 +905,24 @@ def golden_step(name, torch, fraction=1.0):
 
         byt = sum(16 * xc.numel() + 4 * xr.numel() + 8 * xr.shape[0] * (xr.shape[1] // 2 + 1) for xc, xr in data)
         return step, byt, "torch.fft.fft and rfft per length"
+    if name == "c2c3d":
+        # the reference has no 3D path: torch.fft.fftn on the same volume
+        x = torch.complex(torch.randn((512, 512, 512), generator=g), torch.randn((512, 512, 512), generator=g))
+
+        def step():
+            F.fftn(x)
+
+        return step, 16 * x.numel(), "torch.fft.fftn of the 512^3 volume (no 3D path in the reference)"
+    if name == "fp64":
+        # the reference's double-precision entries are stubs: torch.fft in FP64
+        b = rows(2048)
+        x = torch.complex(torch.randn((b, 4096), generator=g, dtype=torch.float64),
+                          torch.randn((b, 4096), generator=g, dtype=torch.float64))
+
+        def step():
+            F.fft(x, dim=1)
+
+        return step, 32 * x.numel(), "torch.fft.fft in complex128 (the reference's Z2Z is a stub)"
     raise SystemExit(f"unknown workload {name}")
 
 
