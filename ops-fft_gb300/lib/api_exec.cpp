@@ -555,7 +555,7 @@ ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* id
 ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_D2Z);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {real_elems(plan) * 8, half_elems(plan) * 16, 8, 16}, false, false,
                        false);
 }
@@ -563,7 +563,7 @@ ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata
 ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleReal* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_Z2D);
-    if (plan->rank != 1) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {half_elems(plan) * 16, real_elems(plan) * 8, 16, 8}, false, false,
                        true);
 }

@@ -20,7 +20,8 @@
 // lib/fft_plan_init_api.cpp:200-209), and 3D plans exist for C2C (the
 // reference's MakePlan3d returns ACLFFT_NOT_IMPLEMENTED, :250-254).  Double
 // precision is planned too (the reference rejects it at plan time,
-// lib/fft_plan_init_api.cpp:132-136): Z2Z at every rank, D2Z/Z2D in 1D.
+// lib/fft_plan_init_api.cpp:132-136): Z2Z at every rank, D2Z/Z2D in 1D and
+// 2D.
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -404,10 +405,6 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) {
-        GFFT_LOG("aclfftMakePlan2d: type=%d has no 2D execution implementation yet", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     plan->rank = 2;
     plan->lengths[0] = nx;
     plan->lengths[1] = ny;
@@ -478,10 +475,6 @@ ACLFFT_API aclfftResult aclfftPlan2d(aclfftHandle* plan, int batch, int nx, int 
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(batch > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) {
-        GFFT_LOG("aclfftPlan2d: type=%d has no 2D execution implementation yet", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     aclfftResult r = aclfftCreate(plan);
     if (r != ACLFFT_SUCCESS) return r;
     r = aclfftMakePlan2d(*plan, batch, nx, ny, type, nullptr);
@@ -550,7 +543,6 @@ ACLFFT_API aclfftResult aclfftGetSize2d(aclfftHandle plan, int nx, int ny, aclff
     ACLFFT_CHECK_PARAM(nx > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_R2C && type != ACLFFT_C2R && type != ACLFFT_Z2Z) return ACLFFT_NOT_SUPPORTED;
     aclfftHandle_t d;
     d.rank = 2;
     d.lengths[0] = nx;

@@ -977,24 +977,44 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
         ws_bytes = ws2_bytes = total * 16;
         return true;
     }
-    if (p.rank != 1 || p.stride > 1) return unsupported("double-precision real transforms are 1D, horizontal");
-    const int64_t n = p.n0, nb = n / 2 + 1;
-    if (!length_supported(n)) return unsupported("length has a prime factor > 47");
+    if (p.rank > 2 || p.stride > 1) return unsupported("double-precision real transforms are 1D or 2D, horizontal");
     const bool d2z = p.kind == Kind::R2C;
-    const int64_t in_bytes = d2z ? p.batch * n * 8 : p.batch * nb * 16;
+    const int64_t nx = p.rank == 2 ? p.n0 : 1;
+    const int64_t n = p.rank == 2 ? p.n1 : p.n0, nb = n / 2 + 1;
+    const int64_t rows = p.batch * nx;
+    if (!length_supported(n) || !length_supported(nx)) return unsupported("length has a prime factor > 47");
+    auto need = [&](int64_t a, int64_t b) {
+        ws_bytes = std::max(ws_bytes, a);
+        ws2_bytes = std::max(ws2_bytes, b);
+    };
+    // 2D: nx-point transforms down the columns of the half spectrum
+    DLayout col;
+    col.split = nb;
+    col.hi = nx * nb;
+    col.lo = 1;
+    col.stride = nb;
+    if (!d2z && nx > 1) {
+        // Z2D: the backward column transforms first, into a workspace
+        const size_t c0 = out.steps.size();
+        if (!axis(nx, p.batch * nb, col, col, col, 0, 0, true, true)) return unsupported("length not decomposable");
+        out.steps[c0].dp.conj_in = 1;
+        out.steps.back().dp.conj_out = 1;
+        need(rows * nb * 16, rows * nb * 16);
+    }
+    const int src = cur;  // the input, or the workspace holding the column result
+    const int64_t in_bytes = d2z ? rows * n * 8 : rows * nb * 16;
     if (n % 2 == 0) {
         // even N: the real row is an L = N/2 complex row; an L-point
         // transform and the even/odd post-process (D2Z), or the Hermitian
         // pre-process and an L-point transform (Z2D), as in the FP32 path
         const int64_t L = n / 2;
-        DLayout rowL, rowH;
+        DLayout rowL;
         rowL.hi = L;
-        rowH.hi = nb;
         const int64_t toff = tb.add_dtable(n);  // W_N^k for the pre/post-process
         Step pp;
         pp.kind = Step::DPASS;
         DPassArgs& a = pp.dp;
-        a.ntf = p.batch;
+        a.ntf = rows;
         a.n = (int32_t)n;
         a.radix = 1;
         a.ns = 1;
@@ -1003,7 +1023,7 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
         a.in_stride = a.out_stride = 1;
         pp.dtw_off = toff;
         if (d2z) {
-            if (!axis(L, p.batch, rowL, rowL, rowL, DIO_PAIR_IN, 0, false, true))
+            if (!axis(L, rows, rowL, rowL, rowL, DIO_PAIR_IN, 0, false, true))
                 return unsupported("length not decomposable");
             a.io = DIO_R2C_POST;
             a.in_hi = L;
@@ -1015,41 +1035,48 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
             a.io = DIO_C2R_PRE;
             a.in_hi = nb;
             a.out_hi = L;
-            pp.src = IN;
-            pp.dst = BUF_WS2;
+            pp.src = src;
+            pp.dst = src == BUF_WS2 ? BUF_WS : BUF_WS2;
             out.steps.push_back(pp);
-            cur = BUF_WS2;
-            if (!axis(L, p.batch, rowL, rowL, rowL, 0, DIO_PAIR_OUT, false)) return unsupported("length not decomposable");
+            cur = pp.dst;
+            if (!axis(L, rows, rowL, rowL, rowL, 0, DIO_PAIR_OUT, false)) return unsupported("length not decomposable");
             out.steps.back().dp.conj_out = 1;  // the backward transform as a forward one
         }
-        ws_bytes = ws2_bytes = p.batch * std::max<int64_t>(L, nb) * 16;
-        return true;
+        need(rows * std::max<int64_t>(L, nb) * 16, rows * std::max<int64_t>(L, nb) * 16);
+    } else {
+        if (src == BUF_OUT) {
+            // in place: input and output rows have different pitches, the
+            // input moves to the second workspace first
+            Step cp;
+            cp.kind = Step::COPY;
+            cp.copy_bytes = in_bytes;
+            cp.src = BUF_OUT;
+            cp.dst = BUF_WS2;
+            out.steps.push_back(cp);
+            cur = BUF_WS2;
+        }
+        DLayout full, half, real;
+        full.hi = n;
+        half.hi = nb;
+        real.hi = n;
+        if (!axis(n, rows, d2z ? real : half, full, d2z ? half : real, d2z ? DIO_REAL_IN : DIO_HERM_IN,
+                  d2z ? DIO_HALF_OUT : DIO_REAL_OUT, false))
+            return unsupported("length not decomposable");
+        need(rows * n * 16, std::max<int64_t>(rows * n * 16, in_bytes));
     }
-    if (inplace) {
-        // input and output rows have different pitches: the input moves to
-        // the second workspace first
-        Step cp;
-        cp.kind = Step::COPY;
-        cp.copy_bytes = in_bytes;
-        cp.src = BUF_OUT;
-        cp.dst = BUF_WS2;
-        out.steps.push_back(cp);
-        cur = BUF_WS2;
-    }
-    DLayout full, half, real;
-    full.hi = n;
-    half.hi = nb;
-    real.hi = n;
-    if (!axis(n, p.batch, d2z ? real : half, full, d2z ? half : real, d2z ? DIO_REAL_IN : DIO_HERM_IN,
-              d2z ? DIO_HALF_OUT : DIO_REAL_OUT, false))
-        return unsupported("length not decomposable");
-    // (the axis starts from the input or its copy in WS2, never from the
-    // output, so its last pass writes the output directly: a copy could not
-    // change the row pitch)
+    // (the rows start from the input, its copy or the column result in a
+    // workspace, never from the output, so their last pass writes the output
+    // directly: a copy could not change the row pitch)
     for (const Step& s : out.steps)
         if (s.kind == Step::COPY && s.dst == BUF_OUT) return false;
-    ws_bytes = p.batch * n * 16;
-    ws2_bytes = std::max<int64_t>(p.batch * n * 16, in_bytes);
+    if (d2z && nx > 1) {
+        // D2Z: the forward column transforms last, over the half spectrum
+        cur = BUF_OUT;
+        if (!axis(nx, p.batch * nb, col, col, col, 0, 0, true)) return unsupported("length not decomposable");
+        for (Step& s : out.steps)
+            if (s.kind == Step::COPY && s.dst == BUF_OUT) s.copy_bytes = rows * nb * 16;
+        need(rows * nb * 16, rows * nb * 16);
+    }
     return true;
 }
 

@@ -104,7 +104,8 @@ def test_plan1d_error_codes_match_reference():
 def test_plan2d_error_codes_match_reference_within_its_domain():
     """The reference only accepts C2C of {32,64,128}^2; elsewhere it returns
     NOT_SUPPORTED where this library plans the transform (documented
-    widening: any C2C size, and R2C/C2R).  Every other code must match."""
+    widening: any C2C size, R2C/C2R, and double precision).  Every other
+    code must match."""
     ref = _ref_lib()
     mine = A.lib()
     for nx in (0, 32, 64, 128, 2048, 7):
@@ -118,7 +119,7 @@ def test_plan2d_error_codes_match_reference_within_its_domain():
                         ref.aclfftDestroy(h1)
                     if c == 0:
                         mine.aclfftDestroy(h2)
-                    if a == A.NOT_SUPPORTED and c == 0 and t in (A.C2C, A.R2C, A.C2R, A.Z2Z):
+                    if a == A.NOT_SUPPORTED and c == 0 and t in (A.C2C, A.R2C, A.C2R, A.Z2Z, A.D2Z, A.Z2D):
                         continue
                     assert a == c, (b, nx, ny, t, a, c)
 
@@ -253,7 +254,7 @@ def test_work_area_queries():
     assert mine.aclfftGetSize1d(h, 64, A.C2C, 0, ctypes.byref(sz)) == A.INVALID_SIZE
     assert mine.aclfftGetSize1d(h, 64, 0x2B, 1, ctypes.byref(sz)) == A.INVALID_TYPE
     assert mine.aclfftGetSize1d(h, 64, A.Z2Z, 1, ctypes.byref(sz)) == A.SUCCESS  # double precision is planned
-    assert mine.aclfftGetSize2d(h, 64, 64, A.D2Z, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize2d(h, 64, 64, A.D2Z, ctypes.byref(sz)) == A.SUCCESS
     assert mine.aclfftGetSize1d(h, (1 << 27) + 1, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_SIZE
     assert mine.aclfftGetSize3d(h, 8, 8, 8, A.R2C, ctypes.byref(sz)) == A.NOT_SUPPORTED
     assert mine.aclfftGetSize3d(h, 8, 0, 8, A.C2C, ctypes.byref(sz)) == A.INVALID_SIZE

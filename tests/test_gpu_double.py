@@ -143,3 +143,30 @@ def test_unaligned_device_pointers_are_rejected():
         torch.cuda.synchronize()
     with A.Plan.plan1d(256, A.C2C, 2) as p:
         assert lib.aclfftExecC2C(p.handle, base + 4, base + 8192, A.FORWARD) == A.UNALIGNED_DATA
+
+
+@pytest.mark.parametrize("b,nx,ny", [(3, 64, 100), (2, 7, 3000), (1, 30, 999), (2, 1, 64), (3, 5, 1), (2, 9, 4),
+                                     (1, 256, 2048)])
+def test_2d_d2z_z2d_vs_fp64(b, nx, ny):
+    """2D double-precision real transforms: rows through the 1D real path,
+    columns as Z2Z passes over the half spectrum (Z2D: columns first), host
+    and device buffers, in place, against the FP64 oracle."""
+    nb = ny // 2 + 1
+    rng = np.random.default_rng(nx * 11 + ny)
+    x = rng.standard_normal((b, nx, ny))
+    X = np.empty((b, nx, nb), dtype=np.complex128)
+    with A.Plan.plan2d(b, nx, ny, A.D2Z) as p:
+        p.exec_d2z(x, X)
+    _ok(X, O.r2c_2d(x), ("2d d2z", b, nx, ny))
+    Y = rng.standard_normal((b, nx, nb)) + 1j * rng.standard_normal((b, nx, nb))
+    y = np.empty((b, nx, ny))
+    with A.Plan.plan2d(b, nx, ny, A.Z2D) as p:
+        p.exec_z2d(Y, y)
+        Yd = torch.from_numpy(Y).to(_dev())
+        buf = torch.zeros(b * nx * nb * 2, dtype=torch.float64, device=_dev())
+        torch.view_as_complex(buf.view(b, nx, nb, 2)).copy_(Yd)
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_z2d(buf, buf)  # in place
+        torch.cuda.synchronize()
+        assert np.array_equal(buf[: b * nx * ny].view(b, nx, ny).cpu().numpy(), y)
+    _ok(y, O.c2r_2d(Y, ny), ("2d z2d", b, nx, ny))
