@@ -456,14 +456,14 @@ ACLFFT_API aclfftResult aclfftExecC2C(aclfftHandle plan, aclfftComplex* idata, a
 ACLFFT_API aclfftResult aclfftExecR2C(aclfftHandle plan, aclfftReal* idata, aclfftComplex* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_R2C);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false, false);
 }
 
 ACLFFT_API aclfftResult aclfftExecC2R(aclfftHandle plan, aclfftComplex* idata, aclfftReal* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_C2R);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false, true);
 }
 
@@ -482,7 +482,7 @@ ACLFFT_API aclfftResult aclfftExecC2CAdjoint(aclfftHandle plan, aclfftComplex* g
 ACLFFT_API aclfftResult aclfftExecR2CAdjoint(aclfftHandle plan, aclfftComplex* gradOut, aclfftReal* gradIn)
 {
     EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_R2C);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 2, gradOut, gradIn, {half_elems(plan) * 8, real_elems(plan) * 4}, false, false,
                        false);
 }
@@ -533,7 +533,7 @@ ACLFFT_API aclfftResult aclfftExecR2CAdjointWeighted(aclfftHandle plan, const ac
 ACLFFT_API aclfftResult aclfftExecC2RAdjoint(aclfftHandle plan, aclfftReal* gradOut, aclfftComplex* gradIn)
 {
     EXEC_PLAN_CHECKS(plan, gradOut, gradIn, ACLFFT_C2R);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 2, gradOut, gradIn, {real_elems(plan) * 4, half_elems(plan) * 8}, false, false,
                        true);
 }
@@ -555,7 +555,7 @@ ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* id
 ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata, aclfftDoubleComplex* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_D2Z);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {real_elems(plan) * 8, half_elems(plan) * 16, 8, 16}, false, false,
                        false);
 }
@@ -563,7 +563,7 @@ ACLFFT_API aclfftResult aclfftExecD2Z(aclfftHandle plan, aclfftDoubleReal* idata
 ACLFFT_API aclfftResult aclfftExecZ2D(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleReal* odata)
 {
     EXEC_PLAN_CHECKS(plan, idata, odata, ACLFFT_Z2D);
-    if (plan->rank < 1 || plan->rank > 2) return ACLFFT_NOT_IMPLEMENTED;
+    if (plan->rank < 1 || plan->rank > 3) return ACLFFT_NOT_IMPLEMENTED;
     return exec_common(plan, 0, idata, odata, {half_elems(plan) * 16, real_elems(plan) * 8, 16, 8}, false, false,
                        true);
 }

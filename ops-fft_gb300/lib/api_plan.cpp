@@ -17,11 +17,10 @@
 // workspace the plan owns, 2D plans accept any C2C size (the reference only
 // has {32,64,128}^2 kernels and returns ACLFFT_NOT_SUPPORTED otherwise) and
 // R2C/C2R (the reference rejects them until its 2D real path lands,
-// lib/fft_plan_init_api.cpp:200-209), and 3D plans exist for C2C (the
-// reference's MakePlan3d returns ACLFFT_NOT_IMPLEMENTED, :250-254).  Double
+// lib/fft_plan_init_api.cpp:200-209), and 3D plans exist for every type
+// (the reference's MakePlan3d returns ACLFFT_NOT_IMPLEMENTED, :250-254).  Double
 // precision is planned too (the reference rejects it at plan time,
-// lib/fft_plan_init_api.cpp:132-136): Z2Z at every rank, D2Z/Z2D in 1D and
-// 2D.
+// lib/fft_plan_init_api.cpp:132-136), at every rank.
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -420,8 +419,8 @@ ACLFFT_API aclfftResult aclfftMakePlan2d(aclfftHandle plan, int batch, int nx, i
     return ACLFFT_SUCCESS;
 }
 
-// 3D C2C of one nx x ny x nz volume (nz fastest), the reference's signature
-// (include/cann_ops_fft.h:260; no batch argument).
+// 3D transform of one nx x ny x nz volume (nz fastest; every type),
+// the reference's signature (include/cann_ops_fft.h:260; no batch argument).
 ACLFFT_API aclfftResult aclfftMakePlan3d(aclfftHandle plan, int nx, int ny, int nz, aclfftType type,
                                          size_t* workSize)
 {
@@ -431,10 +430,6 @@ ACLFFT_API aclfftResult aclfftMakePlan3d(aclfftHandle plan, int nx, int ny, int 
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) {
-        GFFT_LOG("aclfftMakePlan3d: type=%d has no 3D execution implementation", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     plan->rank = 3;
     plan->lengths[0] = nx;
     plan->lengths[1] = ny;
@@ -492,10 +487,6 @@ ACLFFT_API aclfftResult aclfftPlan3d(aclfftHandle* plan, int nx, int ny, int nz,
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) {
-        GFFT_LOG("aclfftPlan3d: type=%d has no 3D execution implementation", (int)type);
-        return ACLFFT_NOT_SUPPORTED;
-    }
     aclfftResult r = aclfftCreate(plan);
     if (r != ACLFFT_SUCCESS) return r;
     r = aclfftMakePlan3d(*plan, nx, ny, nz, type, nullptr);
@@ -563,7 +554,6 @@ ACLFFT_API aclfftResult aclfftGetSize3d(aclfftHandle plan, int nx, int ny, int n
     ACLFFT_CHECK_PARAM(ny > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(nz > 0, ACLFFT_INVALID_SIZE);
     ACLFFT_CHECK_PARAM(valid_type(type), ACLFFT_INVALID_TYPE);
-    if (type != ACLFFT_C2C && type != ACLFFT_Z2Z) return ACLFFT_NOT_SUPPORTED;
     aclfftHandle_t d;
     d.rank = 3;
     d.lengths[0] = nx;

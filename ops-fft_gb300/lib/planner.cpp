@@ -977,29 +977,41 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
         ws_bytes = ws2_bytes = total * 16;
         return true;
     }
-    if (p.rank > 2 || p.stride > 1) return unsupported("double-precision real transforms are 1D or 2D, horizontal");
+    if (p.stride > 1) return unsupported("double-precision real transforms are horizontal");
     const bool d2z = p.kind == Kind::R2C;
-    const int64_t nx = p.rank == 2 ? p.n0 : 1;
-    const int64_t n = p.rank == 2 ? p.n1 : p.n0, nb = n / 2 + 1;
-    const int64_t rows = p.batch * nx;
-    if (!length_supported(n) || !length_supported(nx)) return unsupported("length has a prime factor > 47");
+    const int nd = p.rank;
+    const int64_t dims[3] = {p.n0, nd >= 2 ? p.n1 : 1, nd == 3 ? p.n2 : 1};
+    const int64_t n = dims[nd - 1], nb = n / 2 + 1;
+    int64_t rows = p.batch;  // rows along the fastest axis
+    for (int a = 0; a + 1 < nd; ++a) rows *= dims[a];
+    for (int a = 0; a < nd; ++a)
+        if (!length_supported(dims[a])) return unsupported("length has a prime factor > 47");
     auto need = [&](int64_t a, int64_t b) {
         ws_bytes = std::max(ws_bytes, a);
         ws2_bytes = std::max(ws2_bytes, b);
     };
-    // 2D: nx-point transforms down the columns of the half spectrum
-    DLayout col;
-    col.split = nb;
-    col.hi = nx * nb;
-    col.lo = 1;
-    col.stride = nb;
-    if (!d2z && nx > 1) {
+    // the slower axes: transforms down the columns of the half spectrum,
+    // element stride S = the faster axes' extent (the fastest as nb bins)
+    auto col_axis = [&](int a, bool in_ws) -> bool {
+        int64_t S = nb;
+        for (int b = a + 1; b + 1 < nd; ++b) S *= dims[b];
+        DLayout l;
+        l.split = S;
+        l.hi = dims[a] * S;
+        l.lo = 1;
+        l.stride = S;
+        return axis(dims[a], rows * nb / dims[a], l, l, l, 0, 0, true, in_ws);
+    };
+    if (!d2z) {
         // Z2D: the backward column transforms first, into a workspace
         const size_t c0 = out.steps.size();
-        if (!axis(nx, p.batch * nb, col, col, col, 0, 0, true, true)) return unsupported("length not decomposable");
-        out.steps[c0].dp.conj_in = 1;
-        out.steps.back().dp.conj_out = 1;
-        need(rows * nb * 16, rows * nb * 16);
+        for (int a = nd - 2; a >= 0; --a)
+            if (dims[a] > 1 && !col_axis(a, true)) return unsupported("length not decomposable");
+        if (out.steps.size() > c0) {
+            out.steps[c0].dp.conj_in = 1;
+            out.steps.back().dp.conj_out = 1;
+            need(rows * nb * 16, rows * nb * 16);
+        }
     }
     const int src = cur;  // the input, or the workspace holding the column result
     const int64_t in_bytes = d2z ? rows * n * 8 : rows * nb * 16;
@@ -1069,13 +1081,14 @@ bool build_dsteps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& 
     // directly: a copy could not change the row pitch)
     for (const Step& s : out.steps)
         if (s.kind == Step::COPY && s.dst == BUF_OUT) return false;
-    if (d2z && nx > 1) {
+    if (d2z) {
         // D2Z: the forward column transforms last, over the half spectrum
         cur = BUF_OUT;
-        if (!axis(nx, p.batch * nb, col, col, col, 0, 0, true)) return unsupported("length not decomposable");
+        for (int a = nd - 2; a >= 0; --a)
+            if (dims[a] > 1 && !col_axis(a, false)) return unsupported("length not decomposable");
         for (Step& s : out.steps)
             if (s.kind == Step::COPY && s.dst == BUF_OUT) s.copy_bytes = rows * nb * 16;
-        need(rows * nb * 16, rows * nb * 16);
+        if (nd > 1) need(rows * nb * 16, rows * nb * 16);
     }
     return true;
 }
@@ -1151,16 +1164,27 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
             return true;
         }
 
-        // real 2D: rows of length ny through the 1D real planner, columns
-        // (length nx, stride ny/2+1) over the half spectrum
-        if (nd != 2) return unsupported("3D supports C2C only");
-        const int64_t nx = p.n0, ny = p.n1, nb = ny / 2 + 1;
-        const int64_t half_bytes = p.batch * nx * nb * 8;
+        // real 2D / 3D: rows along the fastest axis through the 1D real
+        // planner, the slower axes as column passes over the half spectrum
+        // (element stride: the product of the faster axes, the fastest
+        // counted as last/2 + 1 bins)
+        const int64_t nb = last / 2 + 1;
+        const int64_t half_bytes = outer * nb * 8;
+        auto col_stride = [&](int a) {
+            int64_t S = nb;
+            for (int b = a + 1; b + 1 < nd; ++b) S *= dims[b];
+            return S;
+        };
+        auto col_items = [&](int a) {
+            int64_t it = p.batch;
+            for (int b = 0; b < a; ++b) it *= dims[b];
+            return it;
+        };
         Problem rows;
         rows.hints = p.hints;
         rows.kind = p.kind;
-        rows.n0 = ny;
-        rows.batch = p.batch * nx;
+        rows.n0 = last;
+        rows.batch = outer;
         rows.weight = p.weight;
         StepList sub;
         int64_t sub_ws = 0, sub_ws2 = 0;
@@ -1171,27 +1195,37 @@ bool build_steps(const Problem& p, bool inplace, TwiddleBuilder& tb, StepList& o
             out.steps = sub.steps;
             need_ws(sub_ws);
             need_ws2(sub_ws2);
-            if (nx > 1 &&
-                !make_axis_steps(nx, nb, p.batch, nx * nb, BUF_OUT, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
-                return unsupported("2D column length not decomposable");
-            if (spare) need_ws(half_bytes);
+            for (int a = nd - 2; a >= 0; --a) {
+                const int64_t n = dims[a], S = col_stride(a);
+                if (n == 1) continue;
+                if (!make_axis_steps(n, S, col_items(a), n * S, BUF_OUT, BUF_OUT, BUF_WS, cap, tb, out.steps, spare))
+                    return unsupported("column length not decomposable");
+                if (spare) need_ws(half_bytes);
+            }
             return true;
         }
         // C2R: backward column transforms of the half spectrum into the
         // second work area (the input stays intact), then the real rows
-        const bool cols = nx > 1;
+        bool cols = false;
+        for (int a = 0; a + 1 < nd; ++a) cols |= dims[a] > 1;
         if (!build_steps(rows, cols ? false : inplace, tb, sub, sub_ws, sub_ws2)) return false;
         if (!sub.supported) return unsupported(sub.why.c_str());
         if (cols) {
-            if (!make_axis_steps(nx, nb, p.batch, nx * nb, IN, BUF_WS2, BUF_WS, cap, tb, out.steps, spare))
-                return unsupported("2D column length not decomposable");
+            int from = IN;
+            for (int a = nd - 2; a >= 0; --a) {
+                const int64_t n = dims[a], S = col_stride(a);
+                if (n == 1) continue;
+                if (!make_axis_steps(n, S, col_items(a), n * S, from, BUF_WS2, BUF_WS, cap, tb, out.steps, spare))
+                    return unsupported("column length not decomposable");
+                if (spare) need_ws(half_bytes);
+                from = BUF_WS2;
+            }
             out.steps.front().col.conj_in = 1;
             out.steps.back().col.conj_out = 1;
             need_ws2(half_bytes);
-            if (spare) need_ws(half_bytes);
             for (Step& s : sub.steps) {
                 if (s.src == BUF_WS2 || s.dst == BUF_WS2)
-                    return unsupported("2D C2R rows of this length need a second work area of their own");
+                    return unsupported("C2R rows of this length need a second work area of their own");
                 if (s.src == BUF_IN) s.src = BUF_WS2;
             }
         }

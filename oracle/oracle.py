@@ -181,6 +181,18 @@ def c2r_2d(X, ny: int) -> np.ndarray:
     return c2r(_c2c_axis(X, -2, +1), ny)
 
 
+def r2c_3d(x) -> np.ndarray:
+    """3D real-to-complex over the last three axes: rows to nz//2+1 bins,
+    then forward C2C along y and x (composed from the pinned 1D oracles)."""
+    return _c2c_axis(_c2c_axis(r2c(x), -2, -1), -3, -1)
+
+
+def c2r_3d(X, nz: int) -> np.ndarray:
+    """Unscaled 3D complex-to-real: backward C2C along x and y of the half
+    spectrum, then rows of nz//2+1 bins to nz samples."""
+    return c2r(_c2c_axis(_c2c_axis(X, -3, +1), -2, +1), nz)
+
+
 def c2c_3d(x, sign: int = -1) -> np.ndarray:
     """Unscaled 3D C2C over the last three axes (fastest first)."""
     y = c2c(np.asarray(x, dtype=np.complex128), sign)

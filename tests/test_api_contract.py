@@ -126,8 +126,8 @@ def test_plan2d_error_codes_match_reference_within_its_domain():
 
 def test_plan3d_error_codes_match_reference_outside_its_stub():
     """The reference's MakePlan3d is a stub (NOT_IMPLEMENTED after Plan3d's
-    argument checks, lib/fft_plan_api.cpp:127-150); here C2C and Z2Z plans
-    and the other types are NOT_SUPPORTED.  Argument-check codes must match."""
+    argument checks, lib/fft_plan_api.cpp:127-150); here every type plans.
+    Argument-check codes must match."""
     ref = _ref_lib()
     mine = A.lib()
     for nx, ny, nz in ((0, 8, 8), (8, -1, 8), (8, 8, 0), (8, 8, 8), (1, 1, 1), (7, 64, 3000)):
@@ -140,7 +140,7 @@ def test_plan3d_error_codes_match_reference_outside_its_stub():
             if c == 0:
                 mine.aclfftDestroy(h2)
             if a == A.NOT_IMPLEMENTED:
-                assert c == (0 if t in (A.C2C, A.Z2Z) else A.NOT_SUPPORTED), (nx, ny, nz, t, c)
+                assert c == 0, (nx, ny, nz, t, c)  # every valid type is planned here
                 continue
             assert a == c, (nx, ny, nz, t, a, c)
     h = ctypes.c_void_p()
@@ -199,9 +199,9 @@ def test_makeplan_twice_and_create_null():
 
 def test_stubs_return_not_implemented():
     """SetStride stays a stub, as in the reference (lib/fft_utils_api.cpp:
-    90-94); 3D plans of real types are NOT_SUPPORTED.  The double-precision
-    execs, stubs in the reference (lib/fft_exec_api.cpp:87-116), are built
-    here and check their arguments like the FP32 ones."""
+    90-94).  The double-precision execs, stubs in the reference
+    (lib/fft_exec_api.cpp:87-116), are built here and check their arguments
+    like the FP32 ones."""
     mine = A.lib()
     h = ctypes.c_void_p()
     assert mine.aclfftSetStride(h, 2) == A.NOT_IMPLEMENTED
@@ -210,8 +210,8 @@ def test_stubs_return_not_implemented():
     assert mine.aclfftExecZ2D(h, None, None) == A.INVALID_VALUE
     for t in (A.R2C, A.C2R, A.D2Z, A.Z2D):
         hp = ctypes.c_void_p()
-        assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, t) == A.NOT_SUPPORTED
-        assert not hp.value
+        assert mine.aclfftPlan3d(ctypes.byref(hp), 8, 8, 8, t) == A.SUCCESS
+        mine.aclfftDestroy(hp)
     buf = np.zeros(64, dtype=np.complex128)
     with A.Plan.plan1d(16, A.Z2Z, 2) as p:
         assert mine.aclfftExecZ2Z(p.handle, buf.ctypes.data, buf.ctypes.data, 7) == A.INVALID_VALUE
@@ -256,7 +256,7 @@ def test_work_area_queries():
     assert mine.aclfftGetSize1d(h, 64, A.Z2Z, 1, ctypes.byref(sz)) == A.SUCCESS  # double precision is planned
     assert mine.aclfftGetSize2d(h, 64, 64, A.D2Z, ctypes.byref(sz)) == A.SUCCESS
     assert mine.aclfftGetSize1d(h, (1 << 27) + 1, A.C2C, 1, ctypes.byref(sz)) == A.INVALID_SIZE
-    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.R2C, ctypes.byref(sz)) == A.NOT_SUPPORTED
+    assert mine.aclfftGetSize3d(h, 8, 8, 8, A.R2C, ctypes.byref(sz)) == A.SUCCESS
     assert mine.aclfftGetSize3d(h, 8, 0, 8, A.C2C, ctypes.byref(sz)) == A.INVALID_SIZE
     assert mine.aclfftGetSize3d(h, 8, 8, 8, A.C2C, None) == A.INVALID_VALUE
     assert mine.aclfftGetSize(h, ctypes.byref(sz)) == A.INVALID_PLAN  # not made yet
@@ -408,9 +408,10 @@ def test_vertical_and_2d_launches_stay_in_bounds():
                     p.check()
     for dims in ((1, 1, 1), (2, 2, 2), (64, 64, 64), (5, 3000, 7), (7, 5, 3000), (3000, 7, 5), (256, 256, 256),
                  (1, 64, 1), (16, 1, 65536), (4, 5000, 6)):
-        with A.Plan.plan3d(*dims) as p:
-            assert p.info().supported, dims
-            p.check()
+        for t in (A.C2C, A.R2C, A.C2R, A.Z2Z, A.D2Z, A.Z2D):
+            with A.Plan.plan3d(*dims, t) as p:
+                assert p.info().supported, (dims, t)
+                p.check()
 
 
 def test_precision_mode_extension():

@@ -45,7 +45,7 @@ int main(void)
     CHECK(aclfftPlan3d(&plan, 8, 8, 8, ACLFFT_C2C) == ACLFFT_SUCCESS);
     CHECK(aclfftDestroy(plan) == ACLFFT_SUCCESS);
     plan = NULL;
-    CHECK(aclfftPlan3d(&plan, 8, 8, 8, ACLFFT_D2Z) == ACLFFT_NOT_SUPPORTED && plan == NULL);
+    CHECK(aclfftPlan3d(&plan, 8, 8, 8, (aclfftType)0x2b) == ACLFFT_INVALID_TYPE && plan == NULL);
     CHECK(aclfftGetSize1d(NULL, 64, ACLFFT_C2C, 1, &ws) == ACLFFT_INVALID_VALUE);
 
     /* per-operator entries: argument checks return aclError codes */

@@ -170,3 +170,20 @@ def test_2d_d2z_z2d_vs_fp64(b, nx, ny):
         torch.cuda.synchronize()
         assert np.array_equal(buf[: b * nx * ny].view(b, nx, ny).cpu().numpy(), y)
     _ok(y, O.c2r_2d(Y, ny), ("2d z2d", b, nx, ny))
+
+
+@pytest.mark.parametrize("dims", [(8, 12, 20), (5, 7, 9), (1, 6, 31)])
+def test_3d_d2z_z2d_vs_fp64(dims):
+    nz = dims[-1]
+    half = dims[:-1] + (nz // 2 + 1,)
+    rng = np.random.default_rng(sum(dims) + 9)
+    x = rng.standard_normal(dims)
+    X = np.empty(half, dtype=np.complex128)
+    with A.Plan.plan3d(*dims, A.D2Z) as p:
+        p.exec_d2z(x, X)
+    _ok(X, O.r2c_3d(x), ("3d d2z", dims))
+    Y = rng.standard_normal(half) + 1j * rng.standard_normal(half)
+    y = np.empty(dims)
+    with A.Plan.plan3d(*dims, A.Z2D) as p:
+        p.exec_z2d(Y, y)
+    _ok(y, O.c2r_3d(Y, nz), ("3d z2d", dims))

@@ -178,3 +178,31 @@ def test_3d_norm_and_adjoint(mode):
     lhs = np.vdot(G.astype(np.complex128), O.c2c_3d(x, -1) * scale)
     rhs = np.vdot(a.astype(np.complex128), x.astype(np.complex128))
     assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (lhs, rhs)
+
+
+@pytest.mark.parametrize("dims", [(8, 12, 20), (5, 7, 9), (16, 1, 64), (1, 6, 31), (64, 64, 64), (3, 5, 4096)])
+def test_3d_r2c_c2r_vs_fp64(dims):
+    """3D real transforms: rows through the 1D real path, then the y and x
+    axes as column passes over the half spectrum (C2R: columns first, into
+    the second work area), against the FP64 oracle, host buffers and in
+    place on the device."""
+    nz = dims[-1]
+    nb = nz // 2 + 1
+    half = dims[:-1] + (nb,)
+    rng = np.random.default_rng(sum(dims) + 5)
+    x = rng.standard_normal(dims).astype(np.float32)
+    X = np.empty(half, dtype=np.complex64)
+    with A.Plan.plan3d(*dims, A.R2C) as p:
+        p.exec_r2c(x, X)
+    _ok(X, O.r2c_3d(x), ("3d r2c", dims))
+    Y = (rng.standard_normal(half) + 1j * rng.standard_normal(half)).astype(np.complex64)
+    y = np.empty(dims, dtype=np.float32)
+    with A.Plan.plan3d(*dims, A.C2R) as p:
+        p.exec_c2r(Y, y)
+        buf = torch.zeros(int(np.prod(half)) * 2, dtype=torch.float32, device=_dev())
+        torch.view_as_complex(buf.view(*half, 2)).copy_(torch.from_numpy(Y).to(_dev()))
+        p.set_stream(torch.cuda.current_stream())
+        p.exec_c2r(buf, buf)  # in place
+        torch.cuda.synchronize()
+        assert np.array_equal(buf[: x.size].view(*dims).cpu().numpy(), y)
+    _ok(y, O.c2r_3d(Y, nz), ("3d c2r", dims))

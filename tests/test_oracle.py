@@ -162,3 +162,14 @@ def test_3d_oracle_agrees_with_numpy(shape):
     n = int(np.prod(shape))
     assert np.abs(O.c2c_3d(x, -1) - np.fft.fftn(x)).max() < 1e-12 * n
     assert np.abs(O.c2c_3d(x, +1) - np.fft.ifftn(x) * n).max() < 1e-12 * n
+
+
+@pytest.mark.parametrize("shape", [(2, 3, 4), (5, 1, 7), (4, 6, 8), (1, 1, 1), (3, 10, 9)])
+def test_3d_real_oracles_agree_with_numpy(shape):
+    rng = np.random.default_rng(sum(shape) + 2)
+    x = rng.standard_normal(shape)
+    n = int(np.prod(shape))
+    X = O.r2c_3d(x)
+    assert np.abs(X - np.fft.rfftn(x)).max() < 1e-12 * n
+    Y = rng.standard_normal(X.shape) + 1j * rng.standard_normal(X.shape)
+    assert np.abs(O.c2r_3d(Y, shape[-1]) - np.fft.irfftn(Y, s=shape, axes=(0, 1, 2)) * n).max() < 1e-11 * n
