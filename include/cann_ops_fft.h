@@ -132,7 +132,7 @@ ACLFFT_API aclfftResult aclfftExecR2C(aclfftHandle plan, aclfftReal* idata, aclf
 ACLFFT_API aclfftResult aclfftExecC2R(aclfftHandle plan, aclfftComplex* idata, aclfftReal* odata);
 
 /* Double precision (stubs in the reference, lib/fft_exec_api.cpp:87-116):
- * Z2Z of rank 1-3 (HORIZONTAL or VERTICAL in 1D), D2Z/Z2D of rank 1-2, same
+ * Z2Z, D2Z and Z2D of rank 1-3 (Z2Z HORIZONTAL or VERTICAL in 1D), same
  * argument checks, layouts and pointer semantics as the FP32 entries, with
  * FP64 arithmetic and FP64 twiddles throughout. */
 ACLFFT_API aclfftResult aclfftExecZ2Z(aclfftHandle plan, aclfftDoubleComplex* idata, aclfftDoubleComplex* odata,

@@ -7,9 +7,11 @@
     X2 = F.rfft2(x2)         # (..., nx, ny) -> (..., nx, ny//2+1)
     y2 = F.irfft2(X2, (nx, ny))
     Z2 = F.fft2(z2); Z3 = F.fftn(z3)   # 2D / 3D C2C over the last axes
+    X3 = F.rfftn(x3)         # (..., nx, ny, nz) -> (..., nx, ny, nz//2+1)
+    y3 = F.irfftn(X3, (nx, ny, nz))
 
-complex128 / float64 tensors run in double precision (Z2Z of rank 1-3,
-D2Z / Z2D in 1D); everything else in single precision.
+complex128 / float64 tensors run in double precision (Z2Z, D2Z and Z2D of
+rank 1-3); everything else in single precision.
 
 Every forward and backward call is one aclfftExec* / aclfftExec*Adjoint call
 on the current torch stream (3D: one call per leading batch item, the 3D
@@ -21,7 +23,8 @@ Gradients follow torch's complex convention (dL/dRe + i dL/dIm): the
 backward of fft is the opposite-direction transform, the backward of rfft is
 the R2C adjoint (C2R of the gradient with interior bins halved) and the
 backward of irfft is the C2R adjoint (R2C of the gradient, interior bins
-doubled); the 2D forms compose the same way along their column axis.
+doubled); the 2D and 3D forms compose the same way along their slower
+axes.
 """
 from __future__ import annotations
 
@@ -220,3 +223,13 @@ def irfft2(X: torch.Tensor, s: tuple) -> torch.Tensor:
 def fftn(x: torch.Tensor, inverse: bool = False) -> torch.Tensor:
     """Unnormalised 3D C2C over the last three axes."""
     return _C2C.apply(x, inverse, 3)
+
+
+def rfftn(x: torch.Tensor) -> torch.Tensor:
+    """3D R2C over the last three axes: (nx, ny, nz) real -> (nx, ny, nz//2+1) bins."""
+    return _R2C.apply(x, 3)
+
+
+def irfftn(X: torch.Tensor, s: tuple) -> torch.Tensor:
+    """Unnormalised 3D C2R (nx * ny * nz * torch.fft.irfftn) to real shape s = (nx, ny, nz)."""
+    return _C2R.apply(X, tuple(int(v) for v in s))

@@ -1,5 +1,5 @@
-"""GPU parity of the double-precision transforms (Z2Z of rank 1-3, D2Z and
-Z2D in 1D) through the C ABI against the FP64 oracle.  The reference declares
+"""GPU parity of the double-precision transforms (Z2Z, D2Z and Z2D of rank
+1-3) through the C ABI against the FP64 oracle.  The reference declares
 these entries and leaves them as stubs, so parity is against the oracle
 only.  Tolerance: rel-L2 <= 1e-12 (FP64 arithmetic and FP64 twiddles; the
 errors seen are ~1e-15)."""

@@ -214,3 +214,31 @@ def test_double_precision_wrappers_and_gradients(F, n):
     assert _rel(y.detach().cpu().numpy(), yt.detach().numpy()) <= 1e-12
     assert _rel(zd.grad.cpu().numpy(), zt.grad.numpy()) <= 1e-12
     assert _rel(xd.grad.cpu().numpy(), xt.grad.numpy()) <= 1e-12
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_rfftn_irfftn_forward_and_gradient(F, dtype):
+    """3D real wrappers in both precisions (batched volumes): values against
+    numpy and gradients of L = sum w|rfftn(x)|^2 + sum v * irfftn(X) against
+    torch's FP64 autograd."""
+    shape = (2, 6, 10, 12)
+    nx, ny, nz = shape[1:]
+    tol = REL if dtype == torch.float32 else 1e-12
+    rng = np.random.default_rng(17)
+    x = rng.standard_normal(shape)
+    w = rng.uniform(0, 1, shape[:-1] + (nz // 2 + 1,))
+    v = rng.standard_normal(shape)
+    xd = torch.tensor(x, dtype=dtype, device="cuda", requires_grad=True)
+    X = F.rfftn(xd)
+    y = F.irfftn(X, (nx, ny, nz))
+    loss = (torch.tensor(w, dtype=dtype, device="cuda") * X.abs() ** 2).sum() + \
+        (torch.tensor(v, dtype=dtype, device="cuda") * y).sum()
+    loss.backward()
+    axes = (-3, -2, -1)
+    assert _rel(X.detach().cpu().numpy(), np.fft.rfftn(x, axes=axes)) <= tol
+    assert _rel(y.detach().cpu().numpy(), x * nx * ny * nz) <= tol
+    xt = torch.tensor(x, requires_grad=True)
+    Xt = torch.fft.rfftn(xt, dim=axes)
+    yt = torch.fft.irfftn(Xt, s=(nx, ny, nz), dim=axes) * (nx * ny * nz)
+    ((torch.tensor(w) * Xt.abs() ** 2).sum() + (torch.tensor(v) * yt).sum()).backward()
+    assert _rel(xd.grad.cpu().numpy(), xt.grad.numpy()) <= tol
