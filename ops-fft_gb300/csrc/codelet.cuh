@@ -319,6 +319,27 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
             flags[1 + s] = 1;
         }
     };
+    // host-mapped input: every thread of the group copies its share of the
+    // same superset with 16-byte cp.async and commits one group per slot
+    // fill (an empty one when there is no transform left), so that waiting
+    // for all but the newest NST-1 groups completes the oldest slot
+    const bool host_in = A.host_in != 0;
+    auto issue_all = [&](int s, int64_t t) {  // every thread of the group
+        if (t < A.ntf) {
+            const uintptr_t src = buf_lo + (uintptr_t)(t * row_bytes);
+            const uintptr_t c0 = src & ~(uintptr_t)15;
+            const uintptr_t c1 = (src + (uintptr_t)row_bytes + 15) & ~(uintptr_t)15;
+            const bool inside = c0 >= buf_lo && c1 <= buf_hi;
+            if (inside) {
+                unsigned char* dst = slots + (int64_t)s * A.stage_bytes;
+                const int nch = (int)((c1 - c0) >> 4);
+                for (int i = tid; i < nch; i += S::NTHR)
+                    cp_async16(dst + 16 * i, reinterpret_cast<const void*>(c0 + 16 * (uintptr_t)i));
+            }
+            if (leader) flags[1 + s] = inside ? 0 : 1;
+        }
+        cp_async_commit();
+    };
     // prologue: thread 0 starts the table copies (plan-owned memory, safe
     // before the wait for the preceding grid), then each group leader starts
     // its input prefetches once that grid is complete; no thread reads the
@@ -346,13 +367,19 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         for (int s = 0; s < NST; ++s) mbar_init(&bars[s], 1);
         flags[0] = 0;
         fence_mbar_init();
-        for (int s = 0; s < NST; ++s) {
-            const int64_t t = gfirst + (int64_t)s * gstride;
-            if (t < A.ntf) issue(s, t);
+        if (!host_in) {
+            for (int s = 0; s < NST; ++s) {
+                const int64_t t = gfirst + (int64_t)s * gstride;
+                if (t < A.ntf) issue(s, t);
+            }
         }
+    }
+    if (host_in) {
+        for (int s = 0; s < NST; ++s) issue_all(s, gfirst + (int64_t)s * gstride);
     }
     __syncthreads();  // the only CTA-wide barrier: barriers initialised
     if (!mbar_wait_bounded(tbar, 0)) {
+        if (host_in) cp_async_wait_all();
         // the tables never arrived: record it and leave after the group's
         // own copies have landed (or their wait ran out as well)
         if (leader) {
@@ -375,7 +402,9 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         const int64_t t = gfirst + it * gstride;
         if (t >= A.ntf) break;
         const int s = (int)(it % NST);
-        if (leader && !flags[1 + s]) {
+        if (host_in) {
+            cp_async_wait_pending(NST - 1);  // this thread's copies into slot s have landed
+        } else if (leader && !flags[1 + s]) {
             if (!mbar_wait_bounded(&bars[s], (phase >> s) & 1u)) flags[0] = 1;
             phase ^= 1u << s;
         }
@@ -395,7 +424,8 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         unsigned char* row = slots + (int64_t)s * A.stage_bytes + (src & 15);
         if (flags[1 + s]) {
             const float* gs = reinterpret_cast<const float*>(src);
-            for (int64_t i = tid; i < row_bytes / 4; i += S::NTHR) reinterpret_cast<float*>(row)[i] = __ldg(gs + i);
+            for (int64_t i = tid; i < row_bytes / 4; i += S::NTHR)
+                reinterpret_cast<float*>(row)[i] = host_in ? gs[i] : __ldg(gs + i);
             group_sync<S>(bar_id);
         }
         // work layouts (padded, 16-byte aligned): WA inside the slot (it
@@ -430,7 +460,9 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         bool refilled = false;
         auto refill = [&]() {
             refilled = true;
-            if (leader) {
+            if (host_in) {
+                issue_all(s, gfirst + (it + NST) * gstride);
+            } else if (leader) {
                 const int64_t nt = gfirst + (it + NST) * gstride;
                 if (nt < A.ntf) {
                     fence_proxy_async_smem();
@@ -565,6 +597,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         }
         if (!refilled) refill();
     }
+    if (host_in) cp_async_wait_all();
 }
 
 // Column tiles: tfpc adjacent columns of a strided axis (column c, element

@@ -84,6 +84,10 @@ struct RowArgs {
     // bins as they are loaded (bin k of transform t times wload[t*wdist + k])
     const float* wload;
     int64_t wdist;
+    // codelets: `in` is host memory mapped into the device's address space
+    // (pinned host buffers): slots are filled by per-thread cp.async instead
+    // of bulk copies
+    int32_t host_in;
 };
 
 // Strided ("column") transforms, optionally one outer Stockham pass of a

@@ -1,5 +1,5 @@
-// pipe_ptx.cuh - inline-PTX helpers for the bulk-copy input pipeline
-// (mbarrier + cp.async.bulk) shared by the row kernels.
+// pipe_ptx.cuh - inline-PTX helpers for the asynchronous input pipelines
+// (mbarrier + cp.async.bulk, and per-thread cp.async) of the row kernels.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -37,6 +37,29 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32
         "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
 }
+
+// Per-thread asynchronous 16-byte copy global -> shared (the non-bulk
+// cp.async: an ordinary load through the SM's load path, usable on host
+// memory mapped into the device's address space), its commit groups, and
+// the wait for all but the newest `pending` groups of the calling thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_pending(int pending)
+{
+    switch (pending) {
+    case 0: asm volatile("cp.async.wait_group 0;" ::: "memory"); break;
+    case 1: asm volatile("cp.async.wait_group 1;" ::: "memory"); break;
+    case 2: asm volatile("cp.async.wait_group 2;" ::: "memory"); break;
+    default: asm volatile("cp.async.wait_group 3;" ::: "memory"); break;
+    }
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 {

@@ -92,7 +92,7 @@ double norm_scale(const aclfftHandle_t* h, bool backward_like)
 }
 
 int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStream_t st, bool c2c, bool inverse,
-                double dscale, const float* wload = nullptr)
+                double dscale, const float* wload = nullptr, bool host_in = false)
 {
     void* bufs[4] = {in, out, impl->ws, impl->ws2};
     const float2* tw = static_cast<const float2*>(impl->tw);
@@ -115,6 +115,7 @@ int launch_list(PlanImpl* impl, const StepList& sl, void* in, void* out, cudaStr
             s.row.in = src;
             s.row.out = dst;
             s.row.err = impl->err;
+            s.row.host_in = (first && host_in) ? 1 : 0;
             if (c2c) {
                 s.row.conj_in = first && inverse;
                 s.row.conj_out = last && inverse;
@@ -300,6 +301,39 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
     return 0;
 }
 
+// The device address of pinned (page-locked, mapped) host memory, or
+// nullptr for any other pointer.
+void* mapped_host(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host buffers the kernel may use in place: both pinned, the plan one
+// codelet launch from the input to the output (the only kernel whose input
+// pipeline runs on host-mapped memory), the ranges disjoint and aligned to
+// the kernel's element.  OPS_FFT_HOST_DIRECT=0 turns it off (staged copies).
+bool host_direct(const StepList& sl, const void* in, const void* out, size_t in_bytes, size_t out_bytes,
+                 size_t in_align, size_t out_align, void** din, void** dout)
+{
+    const char* env = std::getenv("OPS_FFT_HOST_DIRECT");
+    if (env && env[0] == '0') return false;
+    if (sl.steps.size() != 1) return false;
+    const Step& s = sl.steps[0];
+    if (s.kind != Step::ROW || s.row.codelet < 0 || s.src != 0 || s.dst != 1) return false;
+    const char* i0 = static_cast<const char*>(in);
+    const char* o0 = static_cast<const char*>(out);
+    if (i0 < o0 + out_bytes && o0 < i0 + in_bytes) return false;
+    *din = mapped_host(in);
+    *dout = mapped_host(out);
+    return *din && *dout && reinterpret_cast<uintptr_t>(*din) % in_align == 0 &&
+           reinterpret_cast<uintptr_t>(*dout) % out_align == 0;
+}
+
 struct CallShape {
     size_t in_bytes;
     size_t out_bytes;
@@ -357,6 +391,20 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     }
     // host buffers: stage through device memory, return when done
     if (missing_workspace(impl, primary)) return no_workspace();
+    void* hin = nullptr;
+    void* hout = nullptr;
+    if (!din && !dout &&
+        host_direct(primary, in, out, shape.in_bytes, shape.out_bytes, shape.in_align, shape.out_align, &hin, &hout)) {
+        // pinned host buffers: the kernel reads and writes them over the
+        // host link, with the transfers of both directions overlapping for
+        // the whole call (no staging copies, no pipeline fill or drain)
+        if (launch_list(impl, primary, hin, hout, st, c2c, inverse, scale, nullptr, true) != 0) {
+            cudaStreamSynchronize(st);
+            cudaGetLastError();
+            return ACLFFT_EXEC_FAILED;
+        }
+        return drain_error_word(impl, st, nullptr);
+    }
     const size_t need = std::max(shape.in_bytes, shape.out_bytes);
     if (impl->stage_bytes < need) {
         if (impl->stage_a) cudaFree(impl->stage_a);
