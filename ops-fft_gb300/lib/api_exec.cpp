@@ -316,12 +316,21 @@ void* mapped_host(const void* p)
 // Host buffers the kernel may use in place: both pinned, the plan one
 // codelet launch from the input to the output (the only kernel whose input
 // pipeline runs on host-mapped memory), the ranges disjoint and aligned to
-// the kernel's element.  OPS_FFT_HOST_DIRECT=0 turns it off (staged copies).
+// the kernel's element.  By default only calls of at most kHostDirectBytes
+// (input + output) run in place: measured per call on GB300 (pinned
+// buffers, NVLink-C2C host link), in place beats the staged pipeline on
+// small calls (C2C 4096 x 256, 16.8 MB: 164 vs 149 GB/s) and loses on large
+// ones (R2C 1024 x 4096, 33.6 MB: 168 vs 190; R2C 3000 x 4096, 98 MB: 218 vs
+// 239), where the staged pipeline's copy engines move both directions at
+// once.  OPS_FFT_HOST_DIRECT=1 runs every eligible call in place, =0 none.
+constexpr size_t kHostDirectBytes = 24u << 20;
+
 bool host_direct(const StepList& sl, const void* in, const void* out, size_t in_bytes, size_t out_bytes,
                  size_t in_align, size_t out_align, void** din, void** dout)
 {
     const char* env = std::getenv("OPS_FFT_HOST_DIRECT");
     if (env && env[0] == '0') return false;
+    if (!(env && env[0] == '1') && in_bytes + out_bytes > kHostDirectBytes) return false;
     if (sl.steps.size() != 1) return false;
     const Step& s = sl.steps[0];
     if (s.kind != Step::ROW || s.row.codelet < 0 || s.src != 0 || s.dst != 1) return false;

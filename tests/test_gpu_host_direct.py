@@ -1,8 +1,9 @@
 """Pinned host buffers on one-launch codelet plans: the kernel fills its
 input slots from host memory with per-thread asynchronous copies and writes
-its results to host memory directly (no staging copies).  The same kernel
-runs as on device buffers, so results equal the staged path
-(OPS_FFT_HOST_DIRECT=0) bit for bit, and the FP64 oracle within the FP32
+its results to host memory directly (no staging copies).  By default only
+small calls run that way; the tests force it (OPS_FFT_HOST_DIRECT=1) at every
+size.  The same kernel runs as on device buffers, so results equal the staged
+path (OPS_FFT_HOST_DIRECT=0) bit for bit, and the FP64 oracle within the FP32
 tolerance (rel-L2 <= 1e-5)."""
 import os
 
@@ -25,16 +26,34 @@ def _pinned(a: np.ndarray):
     return t
 
 
-def _staged(fn):
+def _with_mode(mode, fn):
     old = os.environ.get("OPS_FFT_HOST_DIRECT")
-    os.environ["OPS_FFT_HOST_DIRECT"] = "0"
+    if mode is None:
+        os.environ.pop("OPS_FFT_HOST_DIRECT", None)
+    else:
+        os.environ["OPS_FFT_HOST_DIRECT"] = mode
     try:
         fn()
     finally:
         if old is None:
-            del os.environ["OPS_FFT_HOST_DIRECT"]
+            os.environ.pop("OPS_FFT_HOST_DIRECT", None)
         else:
             os.environ["OPS_FFT_HOST_DIRECT"] = old
+
+
+def _staged(fn):
+    _with_mode("0", fn)
+
+
+@pytest.fixture(autouse=True)
+def _force_direct():
+    old = os.environ.get("OPS_FFT_HOST_DIRECT")
+    os.environ["OPS_FFT_HOST_DIRECT"] = "1"
+    yield
+    if old is None:
+        os.environ.pop("OPS_FFT_HOST_DIRECT", None)
+    else:
+        os.environ["OPS_FFT_HOST_DIRECT"] = old
 
 
 def _direct_plan(p):
@@ -76,6 +95,8 @@ def test_c2c_pinned_direct_both_directions_and_norm(n, b):
         for d in (A.FORWARD, A.BACKWARD):
             p.exec_c2c(xh, y1, d)
             _staged(lambda: p.exec_c2c(xh, y2, d))
+            assert torch.equal(y1, y2)
+            _with_mode(None, lambda: p.exec_c2c(xh, y2, d))  # the default (size-dependent) choice
             assert torch.equal(y1, y2)
             assert O.errors(y1.numpy(), O.c2c(x.astype(np.complex128), d))["rel_l2"] <= REL
         p.set_norm(A.NORM_ORTHO)
