@@ -13,12 +13,16 @@
 // picks the first entry whose length matches exactly, or the k-th one with
 // OPS_FFT_CODELET_VARIANT=k (entries after the first for a length are
 // variants: other register caps or radix orders; a column pass takes the
-// entry of its length whose launch bound holds the most columns, 8 to 16:
-// entries 23-25 exist for that, the 512- and 1024-point column passes of 2D
-// and 3D transforms, measured 15-34 % faster than the column kernel on
-// 512^3, 64 x 1024^2, 8 x 1024^2 and 64 x 512^2, and entry 25's 16 columns
-// of 512 points (32 threads each) another 12 % on 512^3; 16-column builds
-// for 256 and 1024 points were slower or no faster).  Each entry is
+// entry of its length that holds 8 to 16 columns with the most threads
+// resident per SM, then the most columns: entries 23-26 exist for that, the
+// 512- and 1024-point column passes of 2D and 3D transforms, measured
+// 15-34 % faster than the column kernel on 512^3, 64 x 1024^2, 8 x 1024^2
+// and 64 x 512^2; entry 25's 16 columns of 512 points (32 threads each)
+// another 12 % on 512^3, and entry 26's 8 columns at 3 CTAs per SM (80
+// registers) another 10 % (512^3 2048 -> 1834 us, 64 x 512^2 169 -> 143 us;
+// 2 CTAs per SM 1906 us, 4 CTAs per SM with spills 1845 us); 16-column
+// builds for 256 and 1024 points, and 8 columns of 1024 points at 2 CTAs
+// per SM (8 x 1024^2 83 -> 90 us), were slower).  Each entry is
 // instantiated in its own translation unit (codelet_<id>.cu) so the build
 // runs in parallel.
 #pragma once
@@ -48,5 +52,6 @@
     X(22, 256, 3, 512, 64, 8, 8, 8)            \
     X(23, 512, 1, 512, 64, 8, 8, 8)            \
     X(24, 512, 1, 1024, 64, 16, 16, 4)         \
-    X(25, 512, 1, 512, 32, 8, 8, 8)
-#define GFFT_NUM_CODELETS 26
+    X(25, 512, 1, 512, 32, 8, 8, 8)        \
+    X(26, 256, 3, 512, 32, 8, 8, 8)
+#define GFFT_NUM_CODELETS 27

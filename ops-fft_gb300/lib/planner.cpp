@@ -537,12 +537,14 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
     // plain column passes of a length with a codelet run as column tiles of
     // that codelet (one transform group per column, in-place passes)
     if (Ns == 1 && !staged_out && codelets_enabled()) {
-        // the codelet of this length whose launch bound holds the most
-        // columns, 8 at least and up to 16 (wider tiles read longer row
-        // segments: 16 columns of 512 points, 128-byte segments, ran the
-        // strided axes of a 512^3 C2C 12 % faster than 8); the first such
-        // entry on ties (OPS_FFT_COLTILE_VARIANT=k: the k-th codelet of the
-        // length, tiles of at least 4 columns; tuning experiments)
+        // the codelet of this length whose launch bound holds 8 to 16
+        // columns with the most threads resident per SM (independent CTAs
+        // overlap one tile's loads with another's passes: 8 columns of 512
+        // points at 3 CTAs per SM ran the strided axes of a 512^3 C2C 10 %
+        // faster than 16 columns at one), then the most columns (wider
+        // tiles read longer row segments); the first such entry on ties
+        // (OPS_FFT_COLTILE_VARIANT=k: the k-th codelet of the length, tiles
+        // of at least 4 columns; tuning experiments)
         int id = -1, cl = 0, cn = 0, cr[kMaxPass], cnr = 0, cmaxt = 0, cminb = 0;
         const char* env_cv = std::getenv("OPS_FFT_COLTILE_VARIANT");
         int min_tf = 8;
@@ -554,14 +556,16 @@ bool make_col_step(int64_t n, int64_t S, int64_t items, int64_t D, int Lq, int64
             }
         }
         if (id < 0) {
-            int best_cols = 0;
+            int best_cols = 0, best_res = 0;
             for (int k = 0;; ++k) {
                 const int cand = gfft_codelet_find(Lq, k);
                 if (cand < 0) break;
                 if (gfft_codelet_info(cand, &cl, &cn, cr, &cnr, &cmaxt, &cminb) != 0) continue;
                 const int cols = std::min(16, cmaxt / cn);
-                if (cols >= 8 && cols > best_cols) {
+                const int res = cmaxt * cminb;
+                if (cols >= 8 && (res > best_res || (res == best_res && cols > best_cols))) {
                     best_cols = cols;
+                    best_res = res;
                     id = cand;
                 }
             }
