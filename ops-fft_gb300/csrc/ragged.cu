@@ -15,8 +15,7 @@
 //               L1 = ip.L transforms of x[j + L2*i]) into the workspace.
 //   RAG_P2      `count` rows k1 of the workspace, each multiplied by
 //               W_L^{k1*n2} and transformed (length L2), written to
-//               X[k1 + L1*k2] (or to the second workspace half for R2C)
-//               through shared memory, a run of `count` bins per k2.
+//               X[k1 + L1*k2] (or to the second workspace half for R2C).
 //   RAG_POST    the even/odd post-process of a long even R2C.
 //
 // Waits (P2 on P1, POST on P2) are done by one thread with a clock bound;
@@ -276,27 +275,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) ragged_kernel(const __grid_con
                 c.km = C.L1;
                 c.kmax = C.n / 2;
             }
-            // the last pass stays in shared memory and the item's rows are
-            // stored together: for each k2 its `count` rows k1 .. k1+count-1
-            // are one contiguous run X[k1 + L1*k2], and consecutive threads
-            // take consecutive rows of a run (a store straight from the last
-            // pass would put consecutive threads L1 elements apart)
-            const int fin = run_passes<RMAX>(c, C.ip2, 0, false);
-            const float2* z = c.buf(fin);
-            float2* ob;
-            if (c2c || odd_r2c) ob = reinterpret_cast<float2*>(static_cast<char*>(A.out) + x.out_off) + item.first;
-            else ob = ws + x.ws_off + C.L + item.first;
-            const int cnt = item.count;
-            const int tot = cnt * C.L2;
-            for (int e = threadIdx.x; e < tot; e += kRagThreads) {
-                const int k2 = e / cnt;
-                const int r = e - k2 * cnt;
-                const int64_t o = r + (int64_t)C.L1 * k2;
-                if (c.kmax >= 0 && item.first + o > c.kmax) continue;
-                float2 v = z[r * C.pitch + spad(k2)];
-                if (c.conj_out) v = cconj(v);
-                ob[o] = cscale(v, c.scale);
-            }
+            run_passes<RMAX>(c, C.ip2, 0, true);
         } else {  // RAG_POST
             const RagXform x = A.xf[item.xform];
             const float2* z = ws + x.ws_off + C.L;
