@@ -216,25 +216,13 @@ aclfftResult no_workspace()
     return ACLFFT_NO_WORKSPACE;
 }
 
-// The device address of pinned (page-locked, mapped) host memory, or
-// nullptr for any other pointer.
-void* mapped_host(const void* p)
-{
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
-}
-
 // Host buffers, one row-kernel step: the batch is cut into chunks whose
 // host-to-device copy, kernel and device-to-host copy run on three streams,
 // so copies in both directions overlap the kernels of neighbouring chunks.
 // Returns 0 on success, 1 on failure, -1 when the transform is too small to
 // be worth chunking (the caller then runs the plain staged path).
 int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* out, size_t in_bytes,
-                        size_t out_bytes, size_t out_align, cudaStream_t st, bool c2c, bool inverse, float scale)
+                        size_t out_bytes, cudaStream_t st, bool c2c, bool inverse, float scale)
 {
     const int64_t ntf = step.row.ntf;
     // chunks per exec (OPS_FFT_HOST_CHUNKS, 2..32, default 4): more chunks
@@ -283,22 +271,10 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
     const bool overlap = static_cast<const char*>(in) < static_cast<const char*>(out) + out_bytes &&
                          static_cast<const char*>(out) < static_cast<const char*>(in) + in_bytes;
     if (overlap && cudaStreamWaitEvent(impl->s_out, impl->ev_in[used - 1], 0) != cudaSuccess) return 1;
-    // a pinned output of a disjoint call is written by the kernels directly
-    // (the row kernels store with ordinary stores, which reach host-mapped
-    // memory over the host link), so no device-to-host copy follows them
-    // (OPS_FFT_HOST_OUT=0: staged)
-    char* hout = nullptr;
-    {
-        const char* env = std::getenv("OPS_FFT_HOST_OUT");
-        if (!overlap && !(env && env[0] == '0')) {
-            hout = static_cast<char*>(mapped_host(out));
-            if (hout && reinterpret_cast<uintptr_t>(hout) % out_align) hout = nullptr;
-        }
-    }
     for (int c = 0; c < used; ++c) {
         const int64_t t0 = c * per, t1 = std::min<int64_t>(ntf, t0 + per);
         char* din = static_cast<char*>(impl->stage_a) + t0 * rin;
-        char* dout = hout ? hout + t0 * rout : static_cast<char*>(impl->stage_b) + t0 * rout;
+        char* dout = static_cast<char*>(impl->stage_b) + t0 * rout;
         if (cudaStreamWaitEvent(st, impl->ev_in[c], 0) != cudaSuccess) return 1;
         gfft::RowArgs a = step.row;
         a.tw = tw;
@@ -312,9 +288,7 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
             a.conj_out = inverse;
         }
         a.scale = scale;
-        if (gfft_launch_row(&a, st) != 0) return 1;
-        if (hout) continue;
-        if (cudaEventRecord(impl->ev_k[c], st) != cudaSuccess ||
+        if (gfft_launch_row(&a, st) != 0 || cudaEventRecord(impl->ev_k[c], st) != cudaSuccess ||
             cudaStreamWaitEvent(impl->s_out, impl->ev_k[c], 0) != cudaSuccess ||
             cudaMemcpyAsync(static_cast<char*>(out) + t0 * rout, dout, (t1 - t0) * rout, cudaMemcpyDeviceToHost,
                             impl->s_out) != cudaSuccess)
@@ -325,6 +299,18 @@ int exec_host_pipelined(PlanImpl* impl, const Step& step, const void* in, void* 
         return 1;
     }
     return 0;
+}
+
+// The device address of pinned (page-locked, mapped) host memory, or
+// nullptr for any other pointer.
+void* mapped_host(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
 // Host buffers the kernel may use in place: both pinned, the plan one
@@ -446,8 +432,7 @@ aclfftResult exec_common(aclfftHandle_t* h, int variant, void* in, void* out, Ca
     void* dev_in = din ? in : impl->stage_a;
     void* dev_out = dout ? out : impl->stage_b;
     if (!din && !dout && primary.steps.size() == 1 && primary.steps[0].kind == Step::ROW) {
-        const int rc = exec_host_pipelined(impl, primary.steps[0], in, out, shape.in_bytes, shape.out_bytes,
-                                           shape.out_align, st, c2c,
+        const int rc = exec_host_pipelined(impl, primary.steps[0], in, out, shape.in_bytes, shape.out_bytes, st, c2c,
                                            inverse, (float)scale);
         if (rc > 0) return ACLFFT_EXEC_FAILED;
         if (rc == 0) return drain_error_word(impl, st, nullptr);

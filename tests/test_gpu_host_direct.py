@@ -146,47 +146,3 @@ def test_offsets_and_pageable_buffers():
         yp = np.empty_like(x)
         p.exec_c2c(x, yp, A.FORWARD)
         assert O.errors(yp, exact)["rel_l2"] <= REL
-
-
-def _env(name, value, fn):
-    old = os.environ.get(name)
-    os.environ[name] = value
-    try:
-        fn()
-    finally:
-        if old is None:
-            os.environ.pop(name, None)
-        else:
-            os.environ[name] = old
-
-
-@pytest.mark.parametrize("kind,n,b", [("r2c", 3000, 4096), ("c2r", 3000, 4095), ("c2c", 4096, 2048)])
-def test_pipelined_calls_write_pinned_output_directly(kind, n, b):
-    """Large pinned calls (staged input, OPS_FFT_HOST_DIRECT=0) run the
-    chunked copy pipeline; its kernels store into the pinned output
-    directly unless OPS_FFT_HOST_OUT=0.  Both equal bit for bit and the
-    oracle on a sample of rows."""
-    nb = n // 2 + 1
-    rng = np.random.default_rng(b)
-    if kind == "r2c":
-        x = rng.standard_normal((b, n)).astype(np.float32)
-        shape_out, dt_out, t = (b, nb), torch.complex64, A.R2C
-    elif kind == "c2r":
-        x = (rng.standard_normal((b, nb)) + 1j * rng.standard_normal((b, nb))).astype(np.complex64)
-        shape_out, dt_out, t = (b, n), torch.float32, A.C2R
-    else:
-        x = (rng.standard_normal((b, n)) + 1j * rng.standard_normal((b, n))).astype(np.complex64)
-        shape_out, dt_out, t = (b, n), torch.complex64, A.C2C
-    xh = _pinned(x)
-    y1 = torch.empty(shape_out, dtype=dt_out, pin_memory=True)
-    y2 = torch.empty(shape_out, dtype=dt_out, pin_memory=True)
-    with A.Plan.plan1d(n, t, b) as p:
-        run = {"r2c": lambda y: p.exec_r2c(xh, y), "c2r": lambda y: p.exec_c2r(xh, y),
-               "c2c": lambda y: p.exec_c2c(xh, y, A.FORWARD)}[kind]
-        _with_mode("0", lambda: run(y1))
-        _with_mode("0", lambda: _env("OPS_FFT_HOST_OUT", "0", lambda: run(y2)))
-    assert torch.equal(y1, y2)
-    rows = slice(0, 64)
-    x64 = x[rows].astype(np.float64 if kind == "r2c" else np.complex128)
-    exact = {"r2c": lambda: O.r2c(x64), "c2r": lambda: O.c2r(x64, n), "c2c": lambda: O.c2c(x64, -1)}[kind]()
-    assert O.errors(y1.numpy()[rows], exact)["rel_l2"] <= REL
