@@ -22,7 +22,9 @@
 // registers) another 10 % (512^3 2048 -> 1834 us, 64 x 512^2 169 -> 143 us;
 // 2 CTAs per SM 1906 us, 4 CTAs per SM with spills 1845 us); 16-column
 // builds for 256 and 1024 points, and 8 columns of 1024 points at 2 CTAs
-// per SM (8 x 1024^2 83 -> 90 us), were slower).  Each entry is
+// per SM (32 threads per column, 128 registers: 8 x 1024^2 83 -> 90 us; 64
+// threads per column, 64 registers with a 48-byte spill: 85 -> 93 us,
+// 64 x 1024^2 563 -> 623 us), were slower).  Each entry is
 // instantiated in its own translation unit (codelet_<id>.cu) so the build
 // runs in parallel.
 #pragma once
