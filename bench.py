@@ -25,7 +25,7 @@ copies are inside the timing; `cpu_baseline` times the reference's golden
 path (torch.fft on the host cores) on the same workload.
 
 With the default workload the line also carries, under `config`, the
-BASELINE cfg3 comparison of the split-precision tensor-core forms against
+comparison (C2C N = 65536 and 16384, batch 64) of the split-precision tensor-core forms against
 the FP32 Stockham form with their FP64 errors, the per-length fractions of
 the HBM roofline at N = 4096-65536, and the same step run through the
 torch.autograd wrappers (loss.backward()).
@@ -392,7 +392,7 @@ class C2CWorkload:
 
 
 class OneExecWorkload:
-    """One forward exec per step of a plan beyond the BASELINE configs, for
+    """One forward exec per step of a plan beyond the benchmark configurations, for
     measurement and profiling: ``c2c3d`` a 3D C2C of 512^3 (z rows, then
     512-point column tiles along y and x); ``fp64`` a double-precision Z2Z of
     4096 x 2048 (three FP64 Stockham passes)."""
@@ -1052,7 +1052,7 @@ def nsets_for(set_bytes, l2):
 
 
 def extra_split_tc_forms(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak):
-    """BASELINE cfg3 (C2C N = 65536 and 16384, batch 64) in every arithmetic
+    """C2C N = 65536 and 16384, batch 64, in every arithmetic
     form: plain FP32 Stockham and the TF32x3 / BF16x3 split-precision
     tensor-core forms, each with GB/s, its dominant launch and its rel-L2 /
     max-abs error against torch's complex128 FFT of the same inputs."""
@@ -1073,7 +1073,7 @@ def extra_split_tc_forms(torch, A, dev, stream, timer, nk, reps, warmup, l2, pea
     best_tc = max((k for k in forms if k != "fp32 stockham" and
                    max(e["rel_l2"] for e in forms[k]["fp64_error"].values()) <= 1e-6),
                   key=lambda k: forms[k]["GB/s"], default=None)
-    return {"workload": "C2C N=65536 and N=16384, batch 64, x ~ N(0,1) (BASELINE cfg3)", "forms": forms,
+    return {"workload": "C2C N=65536 and N=16384, batch 64, x ~ N(0,1)", "forms": forms,
             "fp64_reference": "torch.fft.fft in complex128 on the same device inputs",
             "best_split_form_within_1e-6": best_tc,
             "split_beats_fp32_within_1e-6": bool(best_tc and forms[best_tc]["GB/s"] > fp32)}
@@ -1424,7 +1424,7 @@ def main():
         cfg.update(extras)
         line = {"metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": nk,
                 "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, the workload's shapes and distributions)",
                 "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                 "gpu_launches": wl.launches_per_step * nk, "clocks": clk}
         print(json.dumps(line))
@@ -1460,7 +1460,7 @@ def run_reference(args, rank, world):
               f"the workload's batch per step, {cores} threads")
     line = {"metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t / args.steps * 1e3, 3), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, BASELINE shapes)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, the workload's shapes and distributions)",
             "impl": "reference", "config": cfg,
             "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "reference",
                              "sample": sample},

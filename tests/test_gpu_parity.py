@@ -3,7 +3,7 @@ and is compared with the reference's golden vectors (its own compare rule
 and tolerances) and with the FP64 oracle at the tight FP32 bound.
 
 Tolerances (stated here, used below):
-  * plain FP32 Stockham vs FP64 oracle: rel-L2 <= 1e-5 (BASELINE target);
+  * plain FP32 Stockham vs FP64 oracle: rel-L2 <= 1e-5 (the plain-FP32 target);
   * reference golden vectors: the reference's per-case atol/rtol
     (compare_data.py), which are looser.
 """
@@ -210,7 +210,7 @@ def test_fft1_d_large_reference_cases_full_shape(c):
     assert rel <= REL_FP32, (c["name"], "round trip", rel)
 
 
-# --------------------------------------------------- BASELINE configurations
+# ------------------------------------------------ benchmark configurations
 def _uniform_c64(gen, shape):
     re = torch.rand(shape, generator=gen) * 2 - 1
     im = torch.rand(shape, generator=gen) * 2 - 1
@@ -231,7 +231,7 @@ def test_config1_c2c_4096x256_device():
         p.exec_c2c(xd, yd, A.FORWARD)
         torch.cuda.synchronize()
         y = yd.cpu().numpy()
-        _fp64_ok(y, O.c2c(x.numpy(), -1), what="cfg1")
+        _fp64_ok(y, O.c2c(x.numpy(), -1), what="C2C 4096 x 256")
         # same result through host buffers (staging path) and in place
         yh = c2c_host(4096, 256, x.numpy().reshape(-1).copy(), A.FORWARD).reshape(256, 4096)
         assert np.array_equal(yh, y)
@@ -274,7 +274,7 @@ def test_config3_c2c_batch64_device(n):
         p.set_stream(torch.cuda.current_stream())
         p.exec_c2c(xd, yd, A.FORWARD)
         torch.cuda.synchronize()
-        e = _fp64_ok(yd.cpu().numpy(), O.c2c(x.numpy(), -1), what=f"cfg3 {n}")
+        e = _fp64_ok(yd.cpu().numpy(), O.c2c(x.numpy(), -1), what=f"C2C {n} x 64")
         assert e["rel_l2"] < 2e-6
         # in place (uses the plan's workspace routing)
         zd = xd.clone()
