@@ -26,7 +26,8 @@ def _ok(out, exact, what, bound=REL_FP32):
 
 
 REAL_2D = [(2, 64, 128), (3, 7, 3000), (1, 30, 999), (2, 256, 1000), (1, 5, 1), (4, 1, 64), (1, 2048, 2048),
-           (2, 3, 1 << 17), (1, 4, 1 << 20), (5, 9, 8192), (3, 128, 33), (1, 1000, 26624)]
+           (2, 3, 1 << 17), (1, 4, 1 << 20), (5, 9, 8192), (3, 128, 33), (1, 1000, 26624),
+           (3, 512, 300), (2, 1024, 130)]
 
 
 @pytest.mark.parametrize("b,nx,ny", REAL_2D)
@@ -180,7 +181,8 @@ def test_3d_norm_and_adjoint(mode):
     assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (lhs, rhs)
 
 
-@pytest.mark.parametrize("dims", [(8, 12, 20), (5, 7, 9), (16, 1, 64), (1, 6, 31), (64, 64, 64), (3, 5, 4096)])
+@pytest.mark.parametrize("dims", [(8, 12, 20), (5, 7, 9), (16, 1, 64), (1, 6, 31), (64, 64, 64), (3, 5, 4096),
+                                  (4, 512, 96), (512, 8, 30), (256, 256, 256)])
 def test_3d_r2c_c2r_vs_fp64(dims):
     """3D real transforms: rows through the 1D real path, then the y and x
     axes as column passes over the half spectrum (C2R: columns first, into
