@@ -27,8 +27,10 @@ path (torch.fft on the host cores) on the same workload.
 With the default workload the line also carries, under `config`, the
 comparison (C2C N = 65536 and 16384, batch 64) of the split-precision tensor-core forms against
 the FP32 Stockham form with their FP64 errors, the per-length fractions of
-the HBM roofline at N = 4096-65536, and the same step run through the
-torch.autograd wrappers (loss.backward()).
+the HBM roofline at N = 4096-65536, the same step run through the
+torch.autograd wrappers (loss.backward()), the 2D/3D and double-precision
+forms, and the other benchmark configurations (C2C 4096 x 256, the 2D
+2048^2 x 8 step, the ragged launch).
 """
 from __future__ import annotations
 
@@ -1079,6 +1081,34 @@ def extra_split_tc_forms(torch, A, dev, stream, timer, nk, reps, warmup, l2, pea
             "split_beats_fp32_within_1e-6": bool(best_tc and forms[best_tc]["GB/s"] > fp32)}
 
 
+def extra_other_configs(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak):
+    """The remaining benchmark configurations measured in the same run, each
+    its own workload with rotating buffer sets above 2x L2: C2C 4096 x 256,
+    the 2D 2048^2 x 8 forward / inverse / backward step and the ragged
+    10000-transform persistent launch; GB/s of algorithmic bytes, fraction
+    of the measured HBM copy peak, the dominant launch and FP64 errors."""
+    names = {"cfg1": "C2C N=4096 batch=256", "cfg4": "2D C2C 2048x2048 batch=8 forward + inverse + backward",
+             "cfg5": "ragged 10000 transforms (70% C2C / 30% R2C, N in [16, 32768]) in one persistent launch"}
+    out = {}
+    for name, label in names.items():
+        wl = make_workload(name, torch, A, dev, stream, 1)
+        ns = nsets_for(wl.set_bytes, l2)
+        if ns > 1:
+            del wl
+            torch.cuda.empty_cache()
+            wl = make_workload(name, torch, A, dev, stream, ns)
+        ms, _, dom, _ = measure(wl, timer, nk, reps, warmup, torch)
+        gbs = wl.alg_bytes_per_step * nk / (ms / 1e3) / 1e9
+        dom_gbs = wl.dominant[1] / (dom / 1e3) / 1e9
+        out[label] = {"GB/s": round(gbs, 1), "frac_of_measured_hbm": round(gbs / peak, 3),
+                      "ms_per_step": round(ms / nk, 4), "buffer_sets": ns,
+                      "dominant": wl.dominant[0], "dominant_us": round(dom * 1e3, 2),
+                      "dominant_frac_of_measured_hbm": round(dom_gbs / peak, 3), "fp64_error": wl.fp64_errors()}
+        del wl
+        torch.cuda.empty_cache()
+    return out
+
+
 def extra_long_lengths(torch, A, dev, stream, timer, nk, reps, warmup, l2, peak):
     """Batched C2C and R2C at N = 4096, 16384, 65536 with 2^25 complex points
     per C2C launch (inputs far above L2): per-length launch time and fraction
@@ -1394,6 +1424,8 @@ def main():
                                                   peak)
         extras["double_precision"] = extra_double(torch, A, dev, stream, timer, nk, max(5, reps // 4), args.warmup,
                                                   peak)
+        extras["other_configs"] = extra_other_configs(torch, A, dev, stream, timer, nk, max(5, reps // 4),
+                                                      args.warmup, l2, peak)
         wl = make_workload(args.workload, torch, A, dev, stream, 1)
 
     cpu = None
