@@ -22,8 +22,6 @@ struct Bufs {
     int64_t bytes[4];  // in, out, ws, ws2
 };
 
-int spad_host(int i) { return i + (i >> 4); }
-
 bool fail(std::string& why, const std::string& s)
 {
     why = s;

@@ -12,8 +12,6 @@ namespace {
 
 constexpr int kBigPrimes[] = {17, 19, 23, 29, 31, 37, 41, 43, 47};
 
-int spad_host(int i) { return i + (i >> 4); }
-
 int max_threads_for(int rmax) { return rmax <= 16 ? 512 : 256; }
 
 int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
