@@ -254,6 +254,96 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, const float2* Win
     }
 }
 
+// Whether the even-R2C launches of codelet S use the instance whose last
+// pass is fused with the even/odd post-process (codelet_last_r2c): the last
+// radix at most 8 (two butterflies per unit in registers), its NS = L/R
+// even, and the NS/2 units dividing evenly over the group's threads; 1024
+// points and more (shorter transforms were measured slower with it).
+template <class S>
+__host__ __device__ constexpr bool fuse_r2c_spec()
+{
+    constexpr int RL = S::R[S::NP - 1];
+    constexpr int NSL = S::L / RL;
+    return S::NP >= 2 && S::L >= 1024 && RL <= 8 && NSL % 2 == 0 && (NSL / 2) % S::NTHR == 0;
+}
+
+// The last pass of an even R2C fused with the even/odd post-process.  The
+// last pass (radix R, NS = L/R) has butterfly j write Z[j + r*NS]; the
+// mirror of that bin, L - j - r*NS, is output R-1-r of butterfly NS - j.
+// So unit u (1 <= u < NS/2) runs butterflies u and NS - u and holds every
+// pair (k, L - k) of their 2R outputs in registers; unit 0 runs butterflies
+// 0 (bins r*NS: DC/Nyquist, the self-paired L/2, and pairs r, R - r) and
+// NS/2 (pairs r, R-1-r).  Each pair is post-processed and stored to HBM
+// directly:
+//   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i),
+//   X[k] = E + W_N^k O, X[L-k] = conj(E - W_N^k O),
+//   X[0] = Re Z0 + Im Z0, X[L] = Re Z0 - Im Z0,
+// so the pass's output never goes through shared memory and no separate
+// post-process loop reads it back.  Win: the previous pass's output.
+template <class S>
+__device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2* Win, const float2* tw, int tw_off,
+                                                 const float2* post)
+{
+    constexpr int P = S::NP - 1;
+    constexpr int R = S::R[P];
+    constexpr int NS = S::L / R;
+    constexpr int L = S::L;
+    constexpr int UPT = (NS / 2) / S::NTHR;  // units per thread
+    const float sc = c.scale;
+    const float s2 = c.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
+    float2* out = c.out2;
+    // butterfly j of the last pass, outputs in natural order in z[0..R)
+    auto bfly = [&](int j, float2 (&z)[R]) {
+        sfor<R>([&](auto rr) {
+            constexpr int r = decltype(rr)::value;
+            z[r] = Win[cpad<S>(j + r * NS)];
+        });
+        sfor<R - 1>([&](auto rr) {
+            constexpr int r = decltype(rr)::value + 1;
+            z[r] = cmul(z[r], tw[tw_off + j + r * NS]);
+        });
+        DFT<R>::run(z);
+    };
+    // pair (k, L - k) with k < L/2, or the self-paired k = L/2
+    auto pair = [&](int k, float2 zk, float2 zn) {
+        const float2 zc = cconj(zn);
+        const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
+        const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
+        const float2 wo = cmul(post[k], o);
+        out[k] = cscale(cadd(e, wo), s2);
+        if (L - k != k) out[L - k] = cscale(cconj(csub(e, wo)), s2);
+    };
+    sfor<UPT>([&](auto ii) {
+        constexpr int i = decltype(ii)::value;
+        const int u = c.tid + i * S::NTHR;
+        float2 a[R], b[R];
+        if (u == 0) {
+            bfly(0, a);
+            bfly(NS / 2, b);
+            const float2 z0 = a[0];
+            out[0] = make_float2((z0.x + z0.y) * sc, 0.f);
+            out[L] = make_float2((z0.x - z0.y) * sc, 0.f);
+            sfor<R / 2>([&](auto rr) {
+                constexpr int r = decltype(rr)::value;
+                if constexpr (r > 0) pair(r * NS, a[r], a[R - r]);
+            });
+            pair(L / 2, a[R / 2], a[R / 2]);
+            sfor<R / 2>([&](auto rr) {
+                constexpr int r = decltype(rr)::value;
+                pair(NS / 2 + r * NS, b[r], b[R - 1 - r]);
+            });
+        } else {
+            bfly(u, a);
+            bfly(NS - u, b);
+            sfor<R / 2>([&](auto rr) {
+                constexpr int r = decltype(rr)::value;
+                pair(u + r * NS, a[r], b[R - 1 - r]);
+                pair(NS - u + r * NS, b[r], a[R - 1 - r]);
+            });
+        }
+    });
+}
+
 // Shared-memory layout (byte offsets from the dynamic shared base):
 //   [0, 8)                         mbarrier of the table copies
 //   [smem_tw, ...)                 pass tables (CTA-wide), at smem_tw + (src % 16)
@@ -273,8 +363,9 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, const float2* Win
 // when it would reach outside the buffer (first/last row with unaligned
 // ends) the group copies the row with ordinary loads instead.
 // FC2R: the even-C2R instance (pre-process fused into the first pass, see
-// codelet_pass); the plain instance serves every mode.
-template <class S, bool FC2R = false>
+// codelet_pass); FR2C: the even-R2C instance (post-process fused into the
+// last pass, see codelet_last_r2c); the plain instance serves every mode.
+template <class S, bool FC2R = false, bool FR2C = false>
 __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_constant__ RowArgs A)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
@@ -475,7 +566,7 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         // when K-1-i is even (so the last one writes WB) and WA otherwise;
         // without one, every stage runs in place in WA.
         const bool pre = !FC2R && A.io_mode == IO_C2R_EVEN;
-        const int K = (pre ? 1 : 0) + S::NP - (last_global ? 1 : 0);
+        const int K = (pre ? 1 : 0) + S::NP - ((last_global || FR2C) ? 1 : 0);
         auto out_of = [&](int i) { return (pp && ((K - 1 - i) & 1) == 0) ? WB : WA; };
         int stage = 0;
         const float2* cur = WA;  // input of the next stage once the raw row is consumed
@@ -529,6 +620,10 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
         }
         sfor<S::NP>([&](auto pidx) {
             constexpr int P = decltype(pidx)::value;
+            if constexpr (FR2C && P == S::NP - 1) {
+                codelet_last_r2c<S>(c, cur, tw, A.ip.pass[P].tw_off, post);
+                return;
+            }
             const bool global_last = P == S::NP - 1 && last_global;
             float2* Wo = global_last ? WA : out_of(stage);
             // a barrier between loads and stores: in place (the output is the
@@ -543,7 +638,11 @@ __global__ void __launch_bounds__(S::MAXT, S::MINB) codelet_kernel(const __grid_
                 if (pp && ++stage == K) refill();
             }
         });
-        if (A.io_mode == IO_R2C_EVEN) {
+        if constexpr (FR2C) {
+            // the fused last pass read the previous pass's output, which may
+            // sit in the slot: every read precedes its refill
+            if (!refilled) group_sync<S>(bar_id);
+        } else if (A.io_mode == IO_R2C_EVEN) {
             // post-process pairs:
             //   E = (Z[k] + conj Z[L-k])/2, O = (Z[k] - conj Z[L-k])/(2i)
             //   X[k] = E + W^k O, X[L-k] = conj(E - W^k O),

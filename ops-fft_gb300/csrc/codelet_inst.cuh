@@ -29,6 +29,17 @@ constexpr bool fuse_c2r()
     return S::L == 512 || S::L == 1024 || S::L == 2048;
 }
 
+// OPS_FFT_FUSE_R2C=0 keeps even-R2C launches on the plain instance (separate
+// post-process after the last pass) instead of the fused one (read once).
+inline bool fuse_r2c_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("OPS_FFT_FUSE_R2C");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
 }  // namespace gfft
 
 #define GFFT_CODELET_TU(ID)                                                              \
@@ -38,6 +49,9 @@ constexpr bool fuse_c2r()
         using S_ = CodeletSpec<ID>::type;                                                \
         if constexpr (fuse_c2r<S_>())                                                    \
             if (a->io_mode == IO_C2R_EVEN) return launch_codelet_t<S_, true>(a, st);    \
+        if constexpr (fuse_r2c_spec<S_>())                                               \
+            if (a->io_mode == IO_R2C_EVEN && fuse_r2c_enabled())                        \
+                return launch_codelet_t<S_, false, true>(a, st);                        \
         return launch_codelet_t<S_>(a, st);                                              \
     }                                                                                    \
     int launch_coltile_##ID(const ColArgs* a, cudaStream_t st)                           \

@@ -77,7 +77,7 @@ int launch_col_t(const ColArgs* a, cudaStream_t st)
     return (int)launch_pdl(col_kernel<RMAX>, dim3((unsigned)grid), dim3(threads), smem, st, *a);
 }
 
-template <class S, bool FC2R = false>
+template <class S, bool FC2R = false, bool FR2C = false>
 int launch_codelet_t(const RowArgs* a, cudaStream_t st)
 {
     static unsigned long long attr_mask = 0;
@@ -87,11 +87,11 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
         return (int)cudaErrorInvalidValue;
     if (a->smem_bytes <= 0 || a->smem_bytes > kMaxSmemBytes || a->nstage < 1 || a->nstage > 4)
         return (int)cudaErrorInvalidValue;
-    cudaError_t e = ensure_smem_attr(codelet_kernel<S, FC2R>, attr_mask, (size_t)a->smem_bytes);
+    cudaError_t e = ensure_smem_attr(codelet_kernel<S, FC2R, FR2C>, attr_mask, (size_t)a->smem_bytes);
     if (e != cudaSuccess) return (int)e;
     if (threads != last_threads || a->smem_bytes != last_smem) {
         int occ = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, codelet_kernel<S, FC2R>, threads, (size_t)a->smem_bytes);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, codelet_kernel<S, FC2R, FR2C>, threads, (size_t)a->smem_bytes);
         if (e != cudaSuccess) return (int)e;
         last_threads = threads;
         last_smem = a->smem_bytes;
@@ -103,7 +103,7 @@ int launch_codelet_t(const RowArgs* a, cudaStream_t st)
     if (a->grid > 0) grid = a->grid;
     if (grid < 1) grid = 1;
     if (grid > ctas_needed) grid = ctas_needed;
-    return (int)launch_pdl(codelet_kernel<S, FC2R>, dim3((unsigned)grid), dim3(threads), (size_t)a->smem_bytes, st, *a);
+    return (int)launch_pdl(codelet_kernel<S, FC2R, FR2C>, dim3((unsigned)grid), dim3(threads), (size_t)a->smem_bytes, st, *a);
 }
 
 template <class S>
