@@ -292,17 +292,11 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
     const float sc = c.scale;
     const float s2 = c.weight == WEIGHT_STORE_X2 ? 2.f * sc : sc;
     float2* out = c.out2;
-    // butterfly j of the last pass, outputs in natural order in z[0..R)
-    auto bfly = [&](int j, float2 (&z)[R]) {
+    auto load = [&](int j, float2 (&z)[R]) {
         sfor<R>([&](auto rr) {
             constexpr int r = decltype(rr)::value;
             z[r] = Win[cpad<S>(j + r * NS)];
         });
-        sfor<R - 1>([&](auto rr) {
-            constexpr int r = decltype(rr)::value + 1;
-            z[r] = cmul(z[r], tw[tw_off + j + r * NS]);
-        });
-        DFT<R>::run(z);
     };
     // pair (k, L - k) with k < L/2, or the self-paired k = L/2
     auto pair = [&](int k, float2 zk, float2 zn) {
@@ -318,8 +312,16 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
         const int u = c.tid + i * S::NTHR;
         float2 a[R], b[R];
         if (u == 0) {
-            bfly(0, a);
-            bfly(NS / 2, b);
+            // butterfly 0 has no twiddles; butterfly NS/2 has the constants
+            // W_L^{(NS/2) r} = W_{2R}^r
+            load(0, a);
+            load(NS / 2, b);
+            sfor<R - 1>([&](auto rr) {
+                constexpr int r = decltype(rr)::value + 1;
+                b[r] = twc<2 * R, r>(b[r]);
+            });
+            DFT<R>::run(a);
+            DFT<R>::run(b);
             const float2 z0 = a[0];
             out[0] = make_float2((z0.x + z0.y) * sc, 0.f);
             out[L] = make_float2((z0.x - z0.y) * sc, 0.f);
@@ -333,8 +335,18 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
                 pair(NS / 2 + r * NS, b[r], b[R - 1 - r]);
             });
         } else {
-            bfly(u, a);
-            bfly(NS - u, b);
+            // butterfly NS-u's twiddles from butterfly u's table entries:
+            // W_L^{(NS-u) r} = W_R^r conj(W_L^{u r})
+            load(u, a);
+            load(NS - u, b);
+            sfor<R - 1>([&](auto rr) {
+                constexpr int r = decltype(rr)::value + 1;
+                const float2 w = tw[tw_off + u + r * NS];
+                a[r] = cmul(a[r], w);
+                b[r] = twc<R, r>(cmulc(b[r], w));
+            });
+            DFT<R>::run(a);
+            DFT<R>::run(b);
             sfor<R / 2>([&](auto rr) {
                 constexpr int r = decltype(rr)::value;
                 pair(u + r * NS, a[r], b[R - 1 - r]);
