@@ -298,12 +298,12 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
             z[r] = Win[cpad<S>(j + r * NS)];
         });
     };
-    // pair (k, L - k) with k < L/2, or the self-paired k = L/2; w = W_N^k
-    auto pair = [&](int k, float2 zk, float2 zn, float2 w) {
+    // pair (k, L - k) with k < L/2, or the self-paired k = L/2
+    auto pair = [&](int k, float2 zk, float2 zn) {
         const float2 zc = cconj(zn);
         const float2 e = make_float2(0.5f * (zk.x + zc.x), 0.5f * (zk.y + zc.y));
         const float2 o = make_float2(0.5f * (zk.y - zc.y), 0.5f * (zc.x - zk.x));
-        const float2 wo = cmul(w, o);
+        const float2 wo = cmul(post[k], o);
         out[k] = cscale(cadd(e, wo), s2);
         if (L - k != k) out[L - k] = cscale(cconj(csub(e, wo)), s2);
     };
@@ -325,16 +325,14 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
             const float2 z0 = a[0];
             out[0] = make_float2((z0.x + z0.y) * sc, 0.f);
             out[L] = make_float2((z0.x - z0.y) * sc, 0.f);
-            // N = 2L = 2R NS: W_N^{r NS} = W_{2R}^r, W_N^{NS/2 + r NS} = W_{4R}^{2r+1}
-            const float2 one = make_float2(1.f, 0.f);
             sfor<R / 2>([&](auto rr) {
                 constexpr int r = decltype(rr)::value;
-                if constexpr (r > 0) pair(r * NS, a[r], a[R - r], twc<2 * R, r>(one));
+                if constexpr (r > 0) pair(r * NS, a[r], a[R - r]);
             });
-            pair(L / 2, a[R / 2], a[R / 2], twc<4, 1>(one));
+            pair(L / 2, a[R / 2], a[R / 2]);
             sfor<R / 2>([&](auto rr) {
                 constexpr int r = decltype(rr)::value;
-                pair(NS / 2 + r * NS, b[r], b[R - 1 - r], twc<4 * R, 2 * r + 1>(one));
+                pair(NS / 2 + r * NS, b[r], b[R - 1 - r]);
             });
         } else {
             // butterfly NS-u's twiddles from butterfly u's table entries:
@@ -349,14 +347,10 @@ __device__ __forceinline__ void codelet_last_r2c(const PipeCtx& c, const float2*
             });
             DFT<R>::run(a);
             DFT<R>::run(b);
-            // post-process twiddles from one table entry p = W_N^u:
-            // W_N^{u + r NS} = W_{2R}^r p, W_N^{NS - u + r NS} = W_{2R}^{r+1} conj(p)
-            const float2 pu = post[u];
-            const float2 pc = cconj(pu);
             sfor<R / 2>([&](auto rr) {
                 constexpr int r = decltype(rr)::value;
-                pair(u + r * NS, a[r], b[R - 1 - r], twc<2 * R, r>(pu));
-                pair(NS - u + r * NS, b[r], a[R - 1 - r], twc<2 * R, r + 1>(pc));
+                pair(u + r * NS, a[r], b[R - 1 - r]);
+                pair(NS - u + r * NS, b[r], a[R - 1 - r]);
             });
         }
     });
