@@ -258,13 +258,14 @@ __device__ __forceinline__ void codelet_pass(const PipeCtx& c, const float2* Win
 // pass is fused with the even/odd post-process (codelet_last_r2c): the last
 // radix at most 8 (two butterflies per unit in registers), its NS = L/R
 // even, and the NS/2 units dividing evenly over the group's threads; 1024
-// points and more (shorter transforms were measured slower with it).
+// to 4096 points (shorter transforms were measured slower with it, and the
+// 8192-point build's tables do not fit its row plans).
 template <class S>
 __host__ __device__ constexpr bool fuse_r2c_spec()
 {
     constexpr int RL = S::R[S::NP - 1];
     constexpr int NSL = S::L / RL;
-    return S::NP >= 2 && S::L >= 1024 && RL <= 8 && NSL % 2 == 0 && (NSL / 2) % S::NTHR == 0;
+    return S::NP >= 2 && S::L >= 1024 && S::L <= 4096 && RL <= 8 && NSL % 2 == 0 && (NSL / 2) % S::NTHR == 0;
 }
 
 // The last pass of an even R2C fused with the even/odd post-process.  The
