@@ -381,9 +381,8 @@ def test_vertical_large_and_inplace_device():
         _fp64_ok(xd.cpu().numpy(), O.c2c_vertical(x, +1), what=("vertical", n))
 
 
-@pytest.mark.parametrize("n", [1024, 3000, 7, 65536])
-def test_r2c_c2r_inplace_device(n):
-    b = 8
+@pytest.mark.parametrize("n,b", [(1024, 8), (3000, 8), (7, 8), (65536, 8), (2048, 600), (4096, 300)])
+def test_r2c_c2r_inplace_device(n, b):
     rng = np.random.default_rng(n)
     x = rng.standard_normal((b, n)).astype(np.float32)
     buf = torch.zeros(b * (n // 2 + 1) * 2, device=_dev())
@@ -402,7 +401,7 @@ def test_r2c_c2r_inplace_device(n):
     _fp64_ok(y, n * x.astype(np.float64), what=("c2r in place", n))
 
 
-@pytest.mark.parametrize("n,b", [(1024, 4096), (3000, 4096), (1025, 64), (1 << 20, 2)])
+@pytest.mark.parametrize("n,b", [(1024, 4096), (3000, 4096), (1025, 64), (1 << 20, 2), (4096, 2048)])
 def test_host_inplace_r2c_c2r_c2c(n, b):
     """In-place calls on HOST buffers (the reference's documented layout,
     docs/zh/API_Reference/FFT_1D.md:201: one buffer of batch*2*(n/2+1)
